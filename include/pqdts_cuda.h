@@ -1,0 +1,148 @@
+/*
+ * pqdts_cuda.h -- C ABI of libpqdts_cuda.so, the GB300 (sm_103a) drop-in for
+ * the two-metric projected truncated Newton solve of pc2/pqdts.
+ *
+ * Every entry point is extern "C" with plain pointers and fixed-width
+ * scalars only, so it binds from Fortran (iso_c_binding, see
+ * pqdts_gb300/fortran/pqdts_cuda_mod.f90), C/C++ and Python ctypes.
+ *
+ * Conventions
+ *   - Return value: 0 on success, a negative PQDTS_E* code on failure; the
+ *     message is available from pqdts_cuda_last_error().  No entry point
+ *     aborts the process or falls back to a CPU implementation.
+ *   - Host arrays are borrowed only for the duration of the call (copied).
+ *   - X-shaped host arrays are (M, N) column-major, exactly the reference's
+ *     X(M,N) (pqdts.f90:1540); P-shaped arrays are the reference's P(N,D)
+ *     column-major, i.e. (D, N) row-major (pqdts.f90:1528).
+ *   - Indices are 0-based; maxr = -1 marks the full-space representation.
+ *   - A context owns its device memory and one CUDA stream; calls on one
+ *     context must not overlap (single-threaded per context).
+ */
+#ifndef PQDTS_CUDA_H
+#define PQDTS_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct pqdts_ctx pqdts_ctx;
+
+enum {
+  PQDTS_OK = 0,
+  PQDTS_E_ARG = -1,     /* invalid argument (sizes, indices, null pointer) */
+  PQDTS_E_CUDA = -2,    /* CUDA runtime error (message has the details) */
+  PQDTS_E_STATE = -3,   /* call out of order (e.g. no problem set) */
+  PQDTS_E_IO = -4,      /* file could not be read or written */
+  PQDTS_E_NOMEM = -5    /* device allocation failed */
+};
+
+enum { PQDTS_FP64 = 0, PQDTS_MIXED = 1 };
+
+/* Context on CUDA device `device`.  Replaces the process-level set-up of
+ * program pqdts (pqdts.f90:1222-1293). */
+int pqdts_cuda_create(int32_t device, pqdts_ctx** ctx);
+int pqdts_cuda_destroy(pqdts_ctx* ctx);
+/* Copies the last error message (NUL-terminated, truncated to len). */
+int pqdts_cuda_last_error(pqdts_ctx* ctx, char* buf, int64_t len);
+/* Number of CUDA kernels this context has launched so far. */
+int pqdts_cuda_kernel_launches(pqdts_ctx* ctx, int64_t* count);
+/* verbose = 1 prints the reference's stdout lines (iter, newton-pcg, line
+ * search, positivity constraints) exactly as rank 0 of pqdts_omp.x. */
+int pqdts_cuda_set_verbose(pqdts_ctx* ctx, int32_t verbose);
+
+/* Problem from the reference's per-row dense bands of F (Flocalrow0/1 +
+ * Frows, pqdts.f90:77-83, 1357-1363): row d covers columns
+ * band_lo[d]..band_hi[d] (band_lo[d] = -1: empty row) and its values are
+ * consecutive in band_vals.  P_ND is (D, N) row-major.  precision:
+ * PQDTS_FP64 or PQDTS_MIXED (FP32 Hessian products and CG vectors, FP64
+ * gradient, objective, line search, projections). */
+int pqdts_cuda_set_problem(pqdts_ctx* ctx, int64_t M, int64_t N, int64_t D, const int64_t* band_lo,
+                           const int64_t* band_hi, const double* band_vals, const double* P_ND, double gamma,
+                           int32_t precision);
+
+/* Problem from the reference's input files' COO triplets
+ * (read_sparse_from_python, pqdts.f90:1080-1107; band build 1318-1365; P
+ * assembly 1527-1538).  nnzF < 0: F computed internally (1366-1466, needs
+ * M == (D-1)^2).  nnzP < 0: random P from the documented seeded stream.
+ * Duplicate entries overwrite in input order, as in the reference. */
+int pqdts_cuda_set_problem_coo(pqdts_ctx* ctx, int64_t M, int64_t N, int64_t D, int64_t nnzF, const int32_t* F_row,
+                               const int32_t* F_col, const double* F_val, int64_t nnzP, const int32_t* P_row,
+                               const int32_t* P_col, const double* P_val, double gamma, int32_t precision);
+
+/* Problem data inspection: band of F as built (band_lo/hi may be null). */
+int pqdts_cuda_get_bands(pqdts_ctx* ctx, int64_t* band_lo, int64_t* band_hi, int64_t* nnz);
+
+/* Current iterate X (M,N) column-major (pqdts.f90:1834-1838, 1874). */
+int pqdts_cuda_set_x(pqdts_ctx* ctx, const double* X_colmajor);
+int pqdts_cuda_get_x(pqdts_ctx* ctx, double* X_colmajor);
+
+/* Space of the per-operation entry points below: fullspace = 1 is the
+ * reference's tfullspace = .true.; otherwise maxr (M entries, 0-based) is
+ * the max column of each row (pqdts.f90:97, 1970-1983). */
+int pqdts_cuda_set_space(pqdts_ctx* ctx, int32_t fullspace, const int32_t* maxr);
+int pqdts_cuda_get_maxr(pqdts_ctx* ctx, int32_t* maxr);
+
+/* Per-operation entry points on the context's X (parity and benchmarking).
+ * Like the reference, L, dL and conv_test rebuild X's max column first in
+ * the reduced space, and conv_test switches to the full space.  */
+int pqdts_cuda_L(pqdts_ctx* ctx, double* val);                     /* L, pqdts.f90:917-973 */
+int pqdts_cuda_dL(pqdts_ctx* ctx, double* G_colmajor);             /* dL, pqdts.f90:975-1032 */
+int pqdts_cuda_redO(pqdts_ctx* ctx, double* O_ND);                 /* redO local part, 707-736 */
+int pqdts_cuda_BF(pqdts_ctx* ctx, const double* V_colmajor, double* HV_colmajor); /* BF, 246-342 (FP64) */
+int pqdts_cuda_Bdiag(pqdts_ctx* ctx, double* BD_colmajor);         /* Bdiag, 208-244 */
+int pqdts_cuda_doproj(pqdts_ctx* ctx);                              /* doproj, 1120-1140 */
+int pqdts_cuda_doproj2(pqdts_ctx* ctx, double* xmin);              /* doproj2, 1142-1164 */
+int pqdts_cuda_conv_test(pqdts_ctx* ctx, double* conv);            /* conv_test, 1034-1067 */
+
+/* Euclidean projection of `rows` consecutive vectors of length len onto the
+ * unit simplex (host buffers, y and x may alias).  rows = 1 is the drop-in
+ * for simplexproj_condat_(y, x, &len) (condat_simplexproj.c:60, called at
+ * pqdts.f90:1133). */
+int pqdts_cuda_simplexproj(pqdts_ctx* ctx, const double* y, double* x, int64_t len, int64_t rows);
+
+/* Solve statistics filled by the solve entry points (may be null):
+ * [0] final L  [1] final conv  [2] ||der||  [3] outer iterations
+ * [4] CG iterations  [5] line-search L evaluations  [6] FP64 refinement
+ * iterations (mixed precision)  [7] solve seconds (the reference's `min`
+ * timer, pqdts.f90:1922-2168). */
+enum { PQDTS_NSTATS = 8 };
+
+/* One stage `oiter` (1 = full space, 2 = reduced space) of mode 1
+ * (projected gradient, 1934-1951) or mode 2 (two-metric projected truncated
+ * Newton, 1953-2110) up to maxiiter iterations or conv < conv_thres, then the
+ * stage-end conv_test (2139; output >= 3 prints its lambda lines). */
+int pqdts_cuda_run_stage(pqdts_ctx* ctx, int32_t mode, int32_t oiter, int32_t maxiiter, double conv_thres,
+                         int32_t output, double* stats);
+
+/* The minimisation of program pqdts from the first objective (1908-1915)
+ * through stages start_stage..2 (1927-2167).  stage_cb, when not null, runs
+ * after each stage with the current X (M,N column-major) so the host can
+ * write the stage files (2139-2166). */
+typedef void (*pqdts_stage_cb)(void* user, int32_t oiter, const double* X_colmajor);
+int pqdts_cuda_solve(pqdts_ctx* ctx, int32_t mode, int32_t maxiiter, double conv_thres, int32_t start_stage,
+                     int32_t output, pqdts_stage_cb stage_cb, void* user, double* stats);
+
+/* Accumulated GPU time (CUDA events) of a named region of the reference's
+ * timers ("L", "dL", "BF", "CG", "Lalpha_min", "doproj", "doproj2", "min"). */
+int pqdts_cuda_timer(pqdts_ctx* ctx, const char* name, double* seconds, int64_t* count);
+
+/* Batched solve of n_inst independent instances on one device (a gamma sweep
+ * or resampled P matrices, no counterpart in the single-instance reference:
+ * it replaces n_inst separate pqdts_omp.x runs).  Instance k uses
+ * M[k], N[k], D[k], the bands band_lo/hi/vals + offsets, P + offset, gamma[k];
+ * X holds sum_k M[k]*N[k] doubles (column-major per instance, in order),
+ * starting points on entry and results on exit.  stats: PQDTS_NSTATS per
+ * instance. */
+int pqdts_cuda_solve_batch(int32_t device, int32_t n_inst, const int64_t* M, const int64_t* N, const int64_t* D,
+                           const int64_t* band_lo, const int64_t* band_hi, const double* band_vals,
+                           const int64_t* band_row_offset, const int64_t* band_val_offset, const double* P,
+                           const int64_t* P_offset, const double* gamma, int32_t precision, int32_t mode,
+                           int32_t maxiiter, double conv_thres, double* X, double* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PQDTS_CUDA_H */

@@ -1,0 +1,1149 @@
+// libpqdts_cuda.so: context, device memory, operations and the solver loop
+// of the GB300 drop-in for pqdts's mode-1/mode-2 solve, behind the C ABI of
+// include/pqdts_cuda.h.
+//
+// Control flow mirrors program pqdts (pqdts.f90:1908-2167) on the host; all
+// vectors, scalars of the CG recurrence and every reduction stay on the
+// device.  The host reads back only what decides a branch: the CG exit flag
+// (polled once per queued chunk of iterations), the line-search objectives
+// (one read per batch of step lengths), and the convergence value.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/pqdts_cuda.h"
+#include "fortran_io.h"
+#include "kernels.cuh"
+#include "problem_host.h"
+
+namespace pqdts {
+
+// Constants of the reference, float literals promoted as gfortran does.
+const double kDx = (double)1e-5f;          // Lalpha_min*: dx (pqdts.f90:354, 404, 450)
+const double kActiveTol = (double)1e-8f;   // tactivetol (1207)
+const double kFeasTol = (double)1e-12f;    // xmin >= -1e-12 (424, 430)
+const double kStage1Exit = (double)1e-4f;  // |dlalpha| < 1e-4 (1955)
+const double kHuge = std::numeric_limits<double>::max();
+constexpr int kMaxCG = 50;                 // do j = 1, 50 (2036)
+constexpr int kMaxLS = 100;                // do i = 1, 100 (374, 420, 466)
+constexpr int kBatchLS = 8;                // step lengths evaluated per sweep
+constexpr int kElemGrid = 152 * 8;         // elementwise grids: 8 blocks per SM
+
+struct Err : std::runtime_error {
+  int code;
+  Err(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define CK(call)                                                                                        \
+  do {                                                                                                  \
+    cudaError_t e_ = (call);                                                                            \
+    if (e_ != cudaSuccess)                                                                              \
+      throw Err(e_ == cudaErrorMemoryAllocation ? PQDTS_E_NOMEM : PQDTS_E_CUDA,                         \
+                std::string(#call) + ": " + cudaGetErrorString(e_) + " (" + __FILE__ + ":" +            \
+                    std::to_string(__LINE__) + ")");                                                    \
+  } while (0)
+
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    release();
+    if (count == 0) count = 1;
+    CK(cudaMalloc((void**)&p, count * sizeof(T)));
+    n = count;
+  }
+  void upload(const T* h, size_t count, cudaStream_t s) {
+    alloc(count);
+    if (count) CK(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+};
+
+// GPU-time accumulators for the reference's timer names (pqdts.f90:103-186).
+struct GpuTimers {
+  struct Pending {
+    int id;
+    cudaEvent_t a, b;
+  };
+  std::vector<std::string> names;
+  std::vector<double> secs;
+  std::vector<int64_t> counts;
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> pool;
+  cudaStream_t st = nullptr;
+  int id_of(const char* n) {
+    for (size_t i = 0; i < names.size(); ++i)
+      if (names[i] == n) return (int)i;
+    names.push_back(n);
+    secs.push_back(0);
+    counts.push_back(0);
+    return (int)names.size() - 1;
+  }
+  cudaEvent_t ev() {
+    if (!pool.empty()) {
+      cudaEvent_t e = pool.back();
+      pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    return e;
+  }
+  int begin(const char* n) {
+    Pending p{id_of(n), ev(), nullptr};
+    CK(cudaEventRecord(p.a, st));
+    pending.push_back(p);
+    counts[p.id]++;
+    return (int)pending.size() - 1;
+  }
+  void end(int tok) {
+    pending[tok].b = ev();
+    CK(cudaEventRecord(pending[tok].b, st));
+  }
+  void flush() {
+    if (pending.empty()) return;
+    CK(cudaStreamSynchronize(st));
+    for (auto& p : pending) {
+      float ms = 0;
+      if (p.b) {
+        CK(cudaEventElapsedTime(&ms, p.a, p.b));
+        pool.push_back(p.b);
+      }
+      secs[p.id] += ms * 1e-3;
+      pool.push_back(p.a);
+    }
+    pending.clear();
+  }
+  ~GpuTimers() {
+    for (auto& p : pending) {
+      cudaEventDestroy(p.a);
+      if (p.b) cudaEventDestroy(p.b);
+    }
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+};
+
+struct Scope {
+  GpuTimers& t;
+  int tok;
+  Scope(GpuTimers& tt, const char* n) : t(tt), tok(tt.begin(n)) {}
+  ~Scope() { t.end(tok); }
+};
+
+// CG work vectors of one precision.
+template <typename T>
+struct CGBufs {
+  DBuf<T> r, z, p, Hp, V, sn, rs, R2;
+  void alloc(int64_t MN, int64_t M, int64_t DN) {
+    r.alloc(MN);
+    z.alloc(MN);
+    p.alloc(MN);
+    Hp.alloc(MN);
+    V.alloc(MN);
+    sn.alloc(MN);
+    rs.alloc(M);
+    R2.alloc(DN);
+  }
+};
+
+}  // namespace pqdts
+
+struct pqdts_ctx {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  std::string err;
+  int verbose = 0;
+  std::atomic<int64_t> launches{0};
+  pqdts::HostProblem h;
+  int precision = PQDTS_FP64;
+  bool have_problem = false;
+  // problem on the device
+  pqdts::DBuf<int32_t> flo, fw, tidx;
+  pqdts::DBuf<int64_t> foff, tptr;
+  pqdts::DBuf<double> fval, tval, bdiag, P;
+  pqdts::DBuf<float> fval32, tval32;
+  // iterate and work arrays
+  pqdts::DBuf<double> X, G, Xc, R, sn64;
+  pqdts::DBuf<int8_t> ik;
+  pqdts::DBuf<int32_t> maxr;
+  pqdts::CGBufs<double> cg64;
+  pqdts::CGBufs<float> cg32;
+  pqdts::DBuf<double> part, part2, sc, alphas, lsout, cglog;
+  pqdts::DBuf<int> ipart;
+  pqdts::DBuf<long long> icount;
+  double* pin = nullptr;  // pinned host scalars
+  bool fullspace = true;
+  std::vector<int32_t> h_maxr;
+  pqdts::GpuTimers timers;
+  int64_t n_cg = 0, n_lsL = 0, n_refine = 0;
+  bool refine = false;  // mixed precision: FP64 CG from now on
+};
+
+namespace pqdts {
+
+using Ctx = pqdts_ctx;
+
+static DevBands bands_of(Ctx& c) {
+  DevBands b;
+  b.M = (int)c.h.M;
+  b.N = (int)c.h.N;
+  b.D = (int)c.h.D;
+  b.flo = c.flo.p;
+  b.fw = c.fw.p;
+  b.foff = c.foff.p;
+  b.tptr = c.tptr.p;
+  b.tidx = c.tidx.p;
+  return b;
+}
+
+static inline int cdiv(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+static void post_launch(Ctx& c) {
+  c.launches++;
+  CK(cudaGetLastError());
+}
+
+static int elem_grid(int64_t total) { return std::max(1, std::min<int>(kElemGrid, cdiv(total, 256))); }
+
+static void reduce_to(Ctx& c, const double* part, int64_t count, double* out, int B = 1, bool is_min = false,
+                      double init = 0.0, const double* pred = nullptr) {
+  if (is_min) k_reduce<true><<<B, 512, 0, c.st>>>(part, count, out, init, pred);
+  else k_reduce<false><<<B, 512, 0, c.st>>>(part, count, out, init, pred);
+  post_launch(c);
+}
+
+static void read_back(Ctx& c, const double* dev, int count) {
+  CK(cudaMemcpyAsync(c.pin, dev, count * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+}
+
+// ---------------------------------------------------------------------------
+// Problem upload and buffer allocation.
+// ---------------------------------------------------------------------------
+static void setup_device(Ctx& c) {
+  HostProblem& h = c.h;
+  const int64_t M = h.M, N = h.N, D = h.D, MN = M * N;
+  c.flo.upload(h.flo.data(), D, c.st);
+  c.fw.upload(h.fw.data(), D, c.st);
+  c.foff.upload(h.foff.data(), D, c.st);
+  c.fval.upload(h.fval.data(), h.fval.size(), c.st);
+  c.tptr.upload(h.tptr.data(), h.tptr.size(), c.st);
+  c.tidx.upload(h.tidx.data(), h.tidx.size(), c.st);
+  c.tval.upload(h.tval.data(), h.tval.size(), c.st);
+  c.bdiag.upload(h.bdiag.data(), M, c.st);
+  c.P.upload(h.P.data(), h.P.size(), c.st);
+  if (c.precision == PQDTS_MIXED) {
+    std::vector<float> f32(h.fval.begin(), h.fval.end());
+    c.fval32.upload(f32.data(), f32.size(), c.st);
+    std::vector<float> t32(h.tval.begin(), h.tval.end());
+    c.tval32.upload(t32.data(), t32.size(), c.st);
+    c.cg32.alloc(MN, M, D * N);
+  } else {
+    c.fval32.release();
+    c.tval32.release();
+  }
+  c.cg64.alloc(MN, M, D * N);
+  c.X.alloc(MN);
+  c.G.alloc(MN);
+  c.Xc.alloc((size_t)kBatchLS * MN);
+  c.R.alloc(D * N);
+  c.sn64.alloc(MN);
+  c.ik.alloc(MN);
+  c.maxr.alloc(M);
+  const int64_t fwd_parts = (int64_t)cdiv(N, kBX) * cdiv(D, kBY) * kBatchLS;
+  const int64_t np = std::max<int64_t>({fwd_parts, M, (int64_t)kElemGrid * kBatchLS, 1024});
+  c.part.alloc(np);
+  c.part2.alloc(np);
+  c.ipart.alloc(kElemGrid);
+  c.icount.alloc(1);
+  c.sc.alloc(SC_NSC);
+  c.alphas.alloc(kBatchLS);
+  c.lsout.alloc(4 * kBatchLS);
+  c.cglog.alloc(4 * kMaxCG);
+  // Initial X = 1/N (pqdts.f90:1834-1838) and maxr from the seeded stream.
+  std::vector<double> x0(MN, 1.0 / (double)N);
+  CK(cudaMemcpyAsync(c.X.p, x0.data(), MN * 8, cudaMemcpyHostToDevice, c.st));
+  CK(cudaMemcpyAsync(c.maxr.p, c.h_maxr.data(), M * 4, cudaMemcpyHostToDevice, c.st));
+  CK(cudaStreamSynchronize(c.st));
+  c.fullspace = true;
+  c.have_problem = true;
+}
+
+static void need_problem(Ctx& c) {
+  if (!c.have_problem) throw Err(PQDTS_E_STATE, "no problem set (call pqdts_cuda_set_problem first)");
+}
+
+// ---------------------------------------------------------------------------
+// Operations on device arrays.
+// ---------------------------------------------------------------------------
+static void rebuild(Ctx& c, double* X, int B = 1) {
+  const int M = (int)c.h.M, N = (int)c.h.N;
+  k_rebuild<<<dim3(cdiv(M, kRowThreads), B), kRowThreads, 0, c.st>>>(X, (int64_t)M * N, c.maxr.p, M, N);
+  post_launch(c);
+}
+
+// Objective of B stacked, already projected/rebuilt matrices -> lsout[b]
+// (L_red) and lsout[kBatchLS + b] (L_gam); values land in c.pin after sync.
+static void objective_stack(Ctx& c, const double* Xs, int B) {
+  const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
+  DevBands bd = bands_of(c);
+  dim3 grid(cdiv(N, kBX), cdiv(D, kBY), B);
+  k_fwd<double, 2><<<grid, dim3(kBX, kBY), 0, c.st>>>(bd, c.fval.p, Xs, (int64_t)M * N, c.P.p, nullptr, c.part.p, nullptr);
+  post_launch(c);
+  reduce_to(c, c.part.p, (int64_t)grid.x * grid.y, c.lsout.p, B);
+  if (c.h.gam != 0) {
+    const int g = elem_grid((int64_t)(M - 1) * N);
+    k_gamma_part<<<dim3(g, B), 256, 0, c.st>>>(Xs, (int64_t)M * N, M, N, c.h.gam, c.part2.p);
+    post_launch(c);
+    reduce_to(c, c.part2.p, g, c.lsout.p + kBatchLS, B);
+  } else {
+    CK(cudaMemsetAsync(c.lsout.p + kBatchLS, 0, B * sizeof(double), c.st));
+  }
+}
+
+static void fetch_objectives(Ctx& c, int B, double* L) {
+  CK(cudaMemcpyAsync(c.pin, c.lsout.p, 4 * kBatchLS * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+  for (int b = 0; b < B; ++b) L[b] = c.h.gam != 0 ? c.pin[b] + c.pin[kBatchLS + b] : c.pin[b];
+}
+
+// L(X) on the context's X (917-973).
+static double op_L(Ctx& c) {
+  Scope s(c.timers, "L");
+  if (!c.fullspace) rebuild(c, c.X.p);
+  objective_stack(c, c.X.p, 1);
+  double L;
+  fetch_objectives(c, 1, &L);
+  return L;
+}
+
+// dL(X) -> G (975-1032).
+static void op_dL(Ctx& c, double* X, double* G) {
+  Scope s(c.timers, "dL");
+  const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
+  if (!c.fullspace) rebuild(c, X);
+  DevBands bd = bands_of(c);
+  k_fwd<double, 0><<<dim3(cdiv(N, kBX), cdiv(D, kBY), 1), dim3(kBX, kBY), 0, c.st>>>(bd, c.fval.p, X, 0, c.P.p,
+                                                                                     c.R.p, nullptr, nullptr);
+  post_launch(c);
+  const int tb = std::min(256, std::max(32, cdiv(cdiv(N, 4), 32) * 32));
+  k_trans<double, false><<<M, tb, 0, c.st>>>(bd, c.tval.p, c.R.p, X, nullptr, c.maxr.p, c.fullspace ? 0 : 1,
+                                             2.0 * c.h.gam, nullptr, G, nullptr, nullptr, nullptr);
+  post_launch(c);
+}
+
+// sum(a.b) over M*N -> device scalar `out`.
+static void dot_dev(Ctx& c, const double* a, const double* b, double* out) {
+  const int64_t total = c.h.M * c.h.N;
+  const int g = elem_grid(total);
+  k_dot_part<<<g, 256, 0, c.st>>>(total, a, b, c.part.p);
+  post_launch(c);
+  reduce_to(c, c.part.p, g, out);
+}
+
+// Hessian-vector product of one precision: Hp = H p (BF, 246-342); masks the
+// active set and reduces p.Hp into sc[SC_V2] when ik != null.  `pred`
+// points at the CG done flag (null: always run).
+template <typename T>
+static void hvp(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, const int8_t* ik, bool with_dot,
+                const double* pred = nullptr) {
+  const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
+  DevBands bd = bands_of(c);
+  const T* src = c.fullspace ? b.p.p : b.V.p;
+  k_fwd<T, 1><<<dim3(cdiv(N, kBX), cdiv(D, kBY), 1), dim3(kBX, kBY), 0, c.st>>>(bd, fv, src, 0, nullptr, b.R2.p,
+                                                                                nullptr, pred);
+  post_launch(c);
+  const int tb = std::min(256, std::max(32, cdiv(cdiv(N, 4), 32) * 32));
+  k_trans<T, true><<<M, tb, 0, c.st>>>(bd, tv, b.R2.p, b.p.p, c.fullspace ? nullptr : b.rs.p, c.maxr.p,
+                                       c.fullspace ? 0 : 1, (T)(2.0 * c.h.gam), ik, b.Hp.p,
+                                       with_dot ? b.p.p : nullptr, with_dot ? c.part.p : nullptr, pred);
+  post_launch(c);
+  if (with_dot) reduce_to(c, c.part.p, M, c.sc.p + SC_V2, 1, false, 0.0, pred);
+}
+
+// ---------------------------------------------------------------------------
+// Truncated-Newton PCG (2007-2090) on device vectors of type T.
+// ---------------------------------------------------------------------------
+template <typename T>
+static void cg_solve(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, double bdfac, int64_t* nact_out) {
+  const int M = (int)c.h.M, N = (int)c.h.N;
+  const int64_t MN = (int64_t)M * N;
+  const int g = elem_grid(MN);
+  Scope s(c.timers, "CG");
+  k_cg_init<T><<<g, 256, 0, c.st>>>(c.X.p, c.G.p, c.bdiag.p, bdfac, kActiveTol, M, N, c.ik.p, b.r.p, b.z.p, b.p.p,
+                                    b.sn.p, c.part.p, c.part2.p, c.ipart.p);
+  post_launch(c);
+  reduce_to(c, c.part.p, g, c.sc.p + SC_NORM);
+  reduce_to(c, c.part2.p, g, c.sc.p + SC_RZ);
+  k_sum_i<<<1, 256, 0, c.st>>>(c.ipart.p, g, c.icount.p);
+  post_launch(c);
+  k_cg_scalars0<<<1, 1, 0, c.st>>>(c.sc.p);
+  post_launch(c);
+  if (c.verbose) {
+    long long nact = 0;
+    CK(cudaMemcpyAsync(&nact, c.icount.p, sizeof(long long), cudaMemcpyDeviceToHost, c.st));
+    CK(cudaStreamSynchronize(c.st));
+    if (nact_out) *nact_out = nact;
+    ListLine l;
+    l.s("positivity constraints").i8(nact).s("active of").i8(MN).r8((double)nact / (double)MN).print();
+  }
+  int done_iters = 0;
+  int queued = 0;
+  int chunk = 4;
+  for (;;) {
+    for (int k = 0; k < chunk && queued < kMaxCG; ++k, ++queued) {
+      if (queued > 0) {
+        if (c.fullspace) {
+          k_cg_pupdate<T><<<g, 256, 0, c.st>>>(c.sc.p, MN, b.p.p, b.z.p);
+          post_launch(c);
+        } else {
+          k_cg_lift<T><<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(c.sc.p, 1, M, N, b.p.p, b.z.p, c.maxr.p,
+                                                                         b.V.p, b.rs.p);
+          post_launch(c);
+        }
+      } else if (!c.fullspace) {
+        k_cg_lift<T><<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(nullptr, 0, M, N, b.p.p, b.z.p, c.maxr.p, b.V.p,
+                                                                       b.rs.p);
+        post_launch(c);
+      }
+      {
+        Scope sb(c.timers, "BF");
+        hvp<T>(c, b, fv, tv, c.ik.p, true, c.sc.p);
+      }
+      k_cg_step<T><<<g, 256, 0, c.st>>>(c.sc.p, c.bdiag.p, bdfac, M, N, b.p.p, b.Hp.p, b.sn.p, b.r.p, b.z.p, c.part.p,
+                                        c.part2.p);
+      post_launch(c);
+      reduce_to(c, c.part.p, g, c.sc.p + SC_RZ, 1, false, 0.0, c.sc.p);
+      reduce_to(c, c.part2.p, g, c.sc.p + SC_RR, 1, false, 0.0, c.sc.p);
+      k_cg_scalars1<<<1, 1, 0, c.st>>>(c.sc.p, c.cglog.p, kMaxCG);
+      post_launch(c);
+    }
+    read_back(c, c.sc.p, SC_NSC);
+    if (c.pin[SC_DONE] != 0.0 || queued >= kMaxCG) {
+      done_iters = (int)c.pin[SC_ITER];
+      break;
+    }
+    chunk = 8;
+  }
+  c.n_cg += done_iters;
+  if (c.verbose) {
+    std::vector<double> lg(4 * kMaxCG);
+    CK(cudaMemcpyAsync(lg.data(), c.cglog.p, lg.size() * 8, cudaMemcpyDeviceToHost, c.st));
+    CK(cudaStreamSynchronize(c.st));
+    for (int j = 0; j < done_iters; ++j) {
+      ListLine l;
+      l.s("newton-pcg").i4(j + 1).s("sqrt(b2)=").r8(lg[4 * j]).s("eps=").r8(lg[4 * j + 1]).s("b1=").r8(lg[4 * j + 2]);
+      l.s("v2=").r8(lg[4 * j + 3]).print();
+    }
+  }
+}
+
+// Candidates X + alpha_b*S (b < B) projected the way the stage requires and
+// rebuilt as L does, their objectives and (stage 2) xmin into c.pin.
+static void eval_candidates(Ctx& c, const double* al, int B, bool stage2, double* L, double* xmin) {
+  const int M = (int)c.h.M, N = (int)c.h.N;
+  const int64_t MN = (int64_t)M * N;
+  CK(cudaMemcpyAsync(c.alphas.p, al, B * sizeof(double), cudaMemcpyHostToDevice, c.st));
+  if (stage2) {
+    const int gb = cdiv(M, kRowThreads);
+    Scope s(c.timers, "doproj2");
+    k_cand_proj2<<<dim3(gb, B), kRowThreads, 0, c.st>>>(c.X.p, c.sn64.p, c.alphas.p, c.Xc.p, MN, c.maxr.p, M, N, 1,
+                                                         c.part2.p);
+    post_launch(c);
+    reduce_to(c, c.part2.p, gb, c.lsout.p + 2 * kBatchLS, B, true, 0.0);
+  } else {
+    Scope s(c.timers, "doproj");
+    k_simplex<<<dim3(cdiv((int64_t)M * 32, 128), B), 128, 0, c.st>>>(c.X.p, c.sn64.p, c.alphas.p, c.Xc.p, MN, M, N);
+    post_launch(c);
+  }
+  {
+    Scope s(c.timers, "L");
+    objective_stack(c, c.Xc.p, B);
+  }
+  fetch_objectives(c, B, L);
+  for (int b = 0; b < B; ++b) xmin[b] = stage2 ? c.pin[2 * kBatchLS + b] : 0.0;
+  c.n_lsL += B;
+}
+
+// Projected backtracking line search: Lalpha_min_auglag (440-483) in the
+// full space, Lalpha_min2 (394-438) in the reduced space.  Step lengths are
+// evaluated kBatchLS at a time; the reference's sequential accept rule is
+// then applied to them in order, so the chosen alpha is the same.
+static void line_search(Ctx& c, bool stage2, double& alpha, double& dlalpha) {
+  Scope s(c.timers, "Lalpha_min");
+  double al[kBatchLS], L[kBatchLS], xm[kBatchLS];
+  al[0] = 0.0;
+  al[1] = 0.0 + kDx;
+  al[2] = 1.0;
+  eval_candidates(c, al, 3, stage2, L, xm);
+  const double L0 = L[0];
+  const double df = (L[1] - L0) / kDx;
+  dlalpha = df;
+  double lm = kHuge, alphamin = 0.0;
+  // Evaluated probes waiting to be consumed in order; alpha = 1 is ready.
+  double qa[kBatchLS] = {1.0}, qL[kBatchLS] = {L[2]}, qx[kBatchLS] = {xm[2]};
+  int qlen = 1, qpos = 0;
+  double next_a = 1.0 * 0.75;  // alpha of the probe after the queued ones
+  for (int i = 1; i <= kMaxLS; ++i) {
+    if (qpos == qlen) {
+      qlen = std::min(kBatchLS, kMaxLS - i + 1);
+      for (int k = 0; k < qlen; ++k) {
+        qa[k] = next_a;
+        next_a = next_a * 0.75;
+      }
+      eval_candidates(c, qa, qlen, stage2, qL, qx);
+      qpos = 0;
+    }
+    const double alpha_i = qa[qpos], Lp = qL[qpos], xmin = qx[qpos];
+    ++qpos;
+    const bool better = stage2 ? (Lp < lm && xmin >= -kFeasTol) : (Lp < lm);
+    if (better) {
+      lm = Lp;
+      alphamin = alpha_i;
+    }
+    if (c.verbose) {
+      ListLine l;
+      l.s("line search").i8(i).s("L=").r8(Lp).s("alpha=").r8(alpha_i).s("df(0)=").r8(df);
+      if (stage2) l.s("min(X)=").r8(xmin);
+      l.print();
+    }
+    const double armijo = std::fma(0.1 * alpha_i, df, L0);
+    const bool shrink = stage2 ? (Lp > armijo || xmin < -kFeasTol) : (Lp > armijo);
+    if (!shrink) break;
+  }
+  alpha = alphamin;
+}
+
+// conv_test (1034-1067) on the context's X; leaves the full space selected.
+static double op_conv(Ctx& c, bool tprint) {
+  Scope s(c.timers, "conv_test");
+  const int M = (int)c.h.M, N = (int)c.h.N;
+  if (!c.fullspace) rebuild(c, c.X.p);
+  c.fullspace = true;
+  op_dL(c, c.X.p, c.G.p);
+  DBuf<double> lam;
+  if (tprint && c.verbose) lam.alloc(M);
+  k_conv_rows<<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(c.X.p, c.G.p, M, N, c.part.p,
+                                                              (tprint && c.verbose) ? lam.p : nullptr);
+  post_launch(c);
+  reduce_to(c, c.part.p, M, c.sc.p + SC_TMP);
+  read_back(c, c.sc.p + SC_TMP, 1);
+  const double conv = std::sqrt(c.pin[0] / ((double)N * (double)M));
+  if (tprint && c.verbose) {
+    std::vector<double> hl(M), hg((size_t)M * N);
+    CK(cudaMemcpyAsync(hl.data(), lam.p, M * 8, cudaMemcpyDeviceToHost, c.st));
+    CK(cudaMemcpyAsync(hg.data(), c.G.p, (size_t)M * N * 8, cudaMemcpyDeviceToHost, c.st));
+    CK(cudaStreamSynchronize(c.st));
+    for (int i = 0; i < M; ++i) {
+      double m2 = kHuge;
+      for (int n = 0; n < N; ++n) m2 = std::min(m2, hg[(size_t)i * N + n] + hl[i]);
+      ListLine l;
+      l.s("lambda").i8(i + 1).r8(hl[i]).r8(m2).print();
+    }
+  }
+  return conv;
+}
+
+static void set_full_space(Ctx& c) {
+  c.fullspace = true;
+  CK(cudaMemsetAsync(c.maxr.p, 0xff, c.h.M * sizeof(int32_t), c.st));  // maxr = -1
+}
+
+struct SolveState {
+  double L0 = 0, norm_der = 0, conv = 0, alpha = 0, xmin = 0, dlalpha = 0;
+  int64_t outer = 0;
+  double t0 = 0;
+};
+
+static double wall() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// One outer iteration of mode 2 (1953-2136) or mode 1 (1934-1951, 2111-2136).
+static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
+  const int M = (int)c.h.M, N = (int)c.h.N;
+  const int64_t MN = (int64_t)M * N;
+  const int g = elem_grid(MN);
+  if (mode == 1) {
+    c.fullspace = false;
+    k_stage2_start<<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(c.X.p, c.maxr.p, M, N, 0);
+    post_launch(c);
+    op_dL(c, c.X.p, c.G.p);
+    k_neg_copy<<<g, 256, 0, c.st>>>(MN, c.G.p, c.sn64.p);
+    post_launch(c);
+    line_search(c, true, st.alpha, st.dlalpha);
+  } else {
+    c.fullspace = (oiter == 1);
+    if (!c.fullspace) {
+      k_stage2_start<<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(c.X.p, c.maxr.p, M, N, 1);
+      post_launch(c);
+    } else {
+      set_full_space(c);
+    }
+    op_dL(c, c.X.p, c.G.p);
+    const double bdfac = c.fullspace ? 1.0 : 2.0;
+    const bool fp32 = (c.precision == PQDTS_MIXED) && !c.refine;
+    if (fp32) cg_solve<float>(c, c.cg32, c.fval32.p, c.tval32.p, bdfac, nullptr);
+    else cg_solve<double>(c, c.cg64, c.fval.p, c.tval.p, bdfac, nullptr);
+    if (c.precision == PQDTS_MIXED && c.refine) c.n_refine++;
+    op_dL(c, c.X.p, c.G.p);
+    const int32_t* mr = c.fullspace ? nullptr : c.maxr.p;
+    if (fp32) k_twometric<float><<<g, 256, 0, c.st>>>(c.cg32.sn.p, c.G.p, c.ik.p, mr, c.bdiag.p, bdfac, M, N, c.sn64.p);
+    else k_twometric<double><<<g, 256, 0, c.st>>>(c.cg64.sn.p, c.G.p, c.ik.p, mr, c.bdiag.p, bdfac, M, N, c.sn64.p);
+    post_launch(c);
+    line_search(c, !c.fullspace, st.alpha, st.dlalpha);
+    // Mixed precision: once the FP32 Newton direction stops giving progress
+    // the remaining iterations run the CG in FP64 (final refinement).
+    if (c.precision == PQDTS_MIXED && !c.refine && !c.fullspace && (st.alpha == 0.0 || st.dlalpha >= 0.0))
+      c.refine = true;
+  }
+  if (st.alpha != 0.0) {
+    k_axpy<<<g, 256, 0, c.st>>>(MN, st.alpha, c.sn64.p, c.X.p);
+    post_launch(c);
+  }
+  st.xmin = 0.0;
+  if (c.fullspace) {
+    Scope s(c.timers, "doproj");
+    k_simplex<<<dim3(cdiv((int64_t)M * 32, 128), 1), 128, 0, c.st>>>(c.X.p, nullptr, nullptr, c.X.p, MN, M, N);
+    post_launch(c);
+  } else {
+    Scope s(c.timers, "doproj2");
+    const int gb = cdiv(M, kRowThreads);
+    k_cand_proj2<<<dim3(gb, 1), kRowThreads, 0, c.st>>>(c.X.p, nullptr, nullptr, c.X.p, MN, c.maxr.p, M, N, 0,
+                                                         c.part2.p);
+    post_launch(c);
+    reduce_to(c, c.part2.p, gb, c.sc.p + SC_TMP, 1, true, 0.0);
+    read_back(c, c.sc.p + SC_TMP, 1);
+    st.xmin = c.pin[0];
+  }
+  st.L0 = op_L(c);
+  op_dL(c, c.X.p, c.G.p);
+  dot_dev(c, c.G.p, c.G.p, c.sc.p + SC_TMP);
+  read_back(c, c.sc.p + SC_TMP, 1);
+  st.norm_der = c.pin[0];
+  st.conv = op_conv(c, false);
+  st.outer++;
+}
+
+static void print_iter(Ctx& c, int oiter, int iiter, int mode, const SolveState& st, double t1) {
+  if (!c.verbose) return;
+  const double t2 = wall();
+  ListLine l;
+  l.s("iter").i4(oiter).i4(iiter).s("L=").r8(st.L0).s("max(abs(c))").r8(st.xmin).s("conv").r8(st.conv);
+  l.s("||der||=").r8(std::sqrt(st.norm_der)).s("mode=").i4(mode).s("alpha=").r8(st.alpha).s("dlalpha=").r8(st.dlalpha);
+  l.s("dt=").r8(t2 - t1).s("ttot=").r8(t2 - st.t0).print();
+  fflush(stdout);
+}
+
+static void run_stage(Ctx& c, int mode, int oiter, int maxiiter, double conv_thres, int output, SolveState& st) {
+  st.dlalpha = -kHuge;
+  for (int iiter = 1; iiter <= maxiiter; ++iiter) {
+    const double t1 = wall();
+    if (mode == 2 && oiter == 1 && (std::fabs(st.dlalpha) < kStage1Exit || st.dlalpha > 0)) {
+      if (c.verbose) {
+        ListLine l;
+        l.s("stopping inner iteration because dldlpha is small").r8(st.dlalpha).print();
+      }
+      break;
+    }
+    outer_iteration(c, mode, oiter, st);
+    print_iter(c, oiter, iiter, mode, st, t1);
+    if (st.conv < conv_thres) break;
+  }
+  st.conv = op_conv(c, output >= 3);
+  c.timers.flush();
+}
+
+static void get_x_colmajor(Ctx& c, double* out) {
+  const int64_t M = c.h.M, N = c.h.N;
+  std::vector<double> rm((size_t)M * N);
+  CK(cudaMemcpyAsync(rm.data(), c.X.p, rm.size() * 8, cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+  for (int64_t i = 0; i < M; ++i)
+    for (int64_t n = 0; n < N; ++n) out[i + n * M] = rm[(size_t)i * N + n];
+}
+
+static void set_x_colmajor(Ctx& c, const double* in) {
+  const int64_t M = c.h.M, N = c.h.N;
+  std::vector<double> rm((size_t)M * N);
+  for (int64_t i = 0; i < M; ++i)
+    for (int64_t n = 0; n < N; ++n) rm[(size_t)i * N + n] = in[i + n * M];
+  CK(cudaMemcpyAsync(c.X.p, rm.data(), rm.size() * 8, cudaMemcpyHostToDevice, c.st));
+  CK(cudaStreamSynchronize(c.st));
+}
+
+static void download_rowmajor_to_col(Ctx& c, const double* dev, double* out) {
+  const int64_t M = c.h.M, N = c.h.N;
+  std::vector<double> rm((size_t)M * N);
+  CK(cudaMemcpyAsync(rm.data(), dev, rm.size() * 8, cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+  for (int64_t i = 0; i < M; ++i)
+    for (int64_t n = 0; n < N; ++n) out[i + n * M] = rm[(size_t)i * N + n];
+}
+
+static void fill_stats(Ctx& c, const SolveState& st, double secs, double* stats) {
+  if (!stats) return;
+  stats[0] = st.L0;
+  stats[1] = st.conv;
+  stats[2] = std::sqrt(st.norm_der);
+  stats[3] = (double)st.outer;
+  stats[4] = (double)c.n_cg;
+  stats[5] = (double)c.n_lsL;
+  stats[6] = (double)c.n_refine;
+  stats[7] = secs;
+}
+
+static void solve(Ctx& c, int mode, int maxiiter, double conv_thres, int start_stage, int output, pqdts_stage_cb cb,
+                  void* user, double* stats) {
+  need_problem(c);
+  if (mode != 1 && mode != 2) throw Err(PQDTS_E_ARG, "mode must be 1 or 2");
+  if (start_stage < 1 || start_stage > 2) throw Err(PQDTS_E_ARG, "start_stage must be 1 or 2");
+  SolveState st;
+  c.n_cg = c.n_lsL = c.n_refine = 0;
+  c.refine = false;
+  CK(cudaMemcpyAsync(c.maxr.p, c.h_maxr.data(), c.h.M * 4, cudaMemcpyHostToDevice, c.st));
+  // 1908-1915: objective and gradient of the starting point (full space).
+  c.fullspace = true;
+  st.L0 = op_L(c);
+  op_dL(c, c.X.p, c.G.p);
+  dot_dev(c, c.G.p, c.G.p, c.sc.p + SC_TMP);
+  read_back(c, c.sc.p + SC_TMP, 1);
+  st.norm_der = c.pin[0];
+  if (c.verbose) {
+    ListLine l;
+    l.s("iter").i4(0).i4(0).s("L=").r8(st.L0).s("||der||=").r8(std::sqrt(st.norm_der)).s("dt=").r8(0.0).s("ttot=").r8(0.0);
+    l.print();
+  }
+  const double t0 = wall();
+  st.t0 = t0;
+  const int tmin = c.timers.begin("min");
+  for (int oiter = start_stage; oiter <= 2; ++oiter) {
+    run_stage(c, mode, oiter, maxiiter, conv_thres, output, st);
+    if (cb) {
+      std::vector<double> xh((size_t)c.h.M * c.h.N);
+      get_x_colmajor(c, xh.data());
+      cb(user, oiter, xh.data());
+    }
+  }
+  c.timers.end(tmin);
+  c.timers.flush();
+  CK(cudaStreamSynchronize(c.st));
+  fill_stats(c, st, wall() - t0, stats);
+}
+
+// Problem set-up shared by the entry points.
+static void init_problem(Ctx& c, HostProblem&& h, int precision, SeededStream& rng) {
+  if (precision != PQDTS_FP64 && precision != PQDTS_MIXED) throw Err(PQDTS_E_ARG, "precision must be 0 or 1");
+  c.have_problem = false;
+  c.h = std::move(h);
+  finish_problem(c.h);
+  c.h_maxr = initial_maxr(c.h.M, c.h.N, rng);
+  c.precision = precision;
+  setup_device(c);
+}
+
+static void check_sizes(int64_t M, int64_t N, int64_t D) {
+  if (M < 2 || N < 1 || D < 1) throw Err(PQDTS_E_ARG, "need M >= 2, N >= 1, D >= 1");
+  if (M > INT32_MAX || N > INT32_MAX || D > INT32_MAX || M * N >= ((int64_t)1 << 31) || D * N >= ((int64_t)1 << 31))
+    throw Err(PQDTS_E_ARG, "problem too large for 32-bit row indexing");
+}
+
+}  // namespace pqdts
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+using pqdts::Ctx;
+using pqdts::Err;
+
+template <typename F>
+static int guarded(Ctx* c, F&& f) {
+  if (!c) return PQDTS_E_ARG;
+  try {
+    if (c->st) {
+      cudaError_t e = cudaSetDevice(c->device);
+      if (e != cudaSuccess) throw Err(PQDTS_E_CUDA, cudaGetErrorString(e));
+    }
+    f();
+    return PQDTS_OK;
+  } catch (const Err& e) {
+    c->err = e.what();
+    return e.code;
+  } catch (const std::invalid_argument& e) {
+    c->err = e.what();
+    return PQDTS_E_ARG;
+  } catch (const std::bad_alloc&) {
+    c->err = "host allocation failed";
+    return PQDTS_E_NOMEM;
+  } catch (const std::exception& e) {
+    c->err = e.what();
+    return PQDTS_E_CUDA;
+  }
+}
+
+extern "C" {
+
+int pqdts_cuda_create(int32_t device, pqdts_ctx** out) {
+  if (!out) return PQDTS_E_ARG;
+  *out = nullptr;
+  Ctx* c = new (std::nothrow) Ctx();
+  if (!c) return PQDTS_E_NOMEM;
+  c->device = device;
+  int rc = guarded(c, [&] {
+    int n = 0;
+    CK(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) throw Err(PQDTS_E_ARG, "no CUDA device " + std::to_string(device));
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    CK(cudaMallocHost((void**)&c->pin, 64 * sizeof(double)));
+    c->timers.st = c->st;
+  });
+  if (rc != PQDTS_OK) {
+    fprintf(stderr, "pqdts_cuda_create: %s\n", c->err.c_str());
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+    return rc;
+  }
+  *out = c;
+  return PQDTS_OK;
+}
+
+int pqdts_cuda_destroy(pqdts_ctx* c) {
+  if (!c) return PQDTS_E_ARG;
+  cudaSetDevice(c->device);
+  if (c->st) cudaStreamSynchronize(c->st);
+  if (c->pin) cudaFreeHost(c->pin);
+  cudaStream_t st = c->st;
+  delete c;
+  if (st) cudaStreamDestroy(st);
+  return PQDTS_OK;
+}
+
+int pqdts_cuda_last_error(pqdts_ctx* c, char* buf, int64_t len) {
+  if (!c || !buf || len <= 0) return PQDTS_E_ARG;
+  snprintf(buf, (size_t)len, "%s", c->err.c_str());
+  return PQDTS_OK;
+}
+
+int pqdts_cuda_kernel_launches(pqdts_ctx* c, int64_t* count) {
+  if (!c || !count) return PQDTS_E_ARG;
+  *count = c->launches.load();
+  return PQDTS_OK;
+}
+
+int pqdts_cuda_set_verbose(pqdts_ctx* c, int32_t v) {
+  if (!c) return PQDTS_E_ARG;
+  c->verbose = v;
+  return PQDTS_OK;
+}
+
+int pqdts_cuda_set_problem(pqdts_ctx* c, int64_t M, int64_t N, int64_t D, const int64_t* lo, const int64_t* hi,
+                           const double* vals, const double* P, double gamma, int32_t precision) {
+  return guarded(c, [&] {
+    pqdts::check_sizes(M, N, D);
+    if (!lo || !hi || !P) throw Err(PQDTS_E_ARG, "null band or P pointer");
+    pqdts::HostProblem h;
+    h.M = M;
+    h.N = N;
+    h.D = D;
+    h.gam = gamma;
+    int64_t tot = 0;
+    for (int64_t d = 0; d < D; ++d)
+      if (lo[d] >= 0) tot += hi[d] - lo[d] + 1;
+    if (tot > 0 && !vals) throw Err(PQDTS_E_ARG, "null band values");
+    pqdts::bands_from_bands(h, lo, hi, vals);
+    h.P.assign(P, P + (size_t)D * N);
+    pqdts::SeededStream rng;
+    pqdts::init_problem(*c, std::move(h), precision, rng);
+  });
+}
+
+int pqdts_cuda_set_problem_coo(pqdts_ctx* c, int64_t M, int64_t N, int64_t D, int64_t nnzF, const int32_t* Fr,
+                               const int32_t* Fc, const double* Fv, int64_t nnzP, const int32_t* Pr, const int32_t* Pc,
+                               const double* Pv, double gamma, int32_t precision) {
+  return guarded(c, [&] {
+    pqdts::check_sizes(M, N, D);
+    pqdts::HostProblem h;
+    h.M = M;
+    h.N = N;
+    h.D = D;
+    h.gam = gamma;
+    if (nnzF >= 0) {
+      if (nnzF > 0 && (!Fr || !Fc || !Fv)) throw Err(PQDTS_E_ARG, "null F arrays");
+      pqdts::bands_from_coo(h, nnzF, Fr, Fc, Fv);
+    } else {
+      pqdts::bands_internal(h);
+    }
+    if (nnzP > 0 && (!Pr || !Pc || !Pv)) throw Err(PQDTS_E_ARG, "null P arrays");
+    pqdts::SeededStream rng;
+    pqdts::P_from_coo(h, nnzP, Pr, Pc, Pv, rng);
+    pqdts::init_problem(*c, std::move(h), precision, rng);
+  });
+}
+
+int pqdts_cuda_get_bands(pqdts_ctx* c, int64_t* lo, int64_t* hi, int64_t* nnz) {
+  return guarded(c, [&] {
+    pqdts::need_problem(*c);
+    for (int64_t d = 0; d < c->h.D; ++d) {
+      if (lo) lo[d] = c->h.flo[d];
+      if (hi) hi[d] = c->h.flo[d] < 0 ? -1 : c->h.flo[d] + c->h.fw[d] - 1;
+    }
+    if (nnz) *nnz = c->h.nnz();
+  });
+}
+
+int pqdts_cuda_set_x(pqdts_ctx* c, const double* X) {
+  return guarded(c, [&] {
+    pqdts::need_problem(*c);
+    if (!X) throw Err(PQDTS_E_ARG, "null X");
+    pqdts::set_x_colmajor(*c, X);
+  });
+}
+
+int pqdts_cuda_get_x(pqdts_ctx* c, double* X) {
+  return guarded(c, [&] {
+    pqdts::need_problem(*c);
+    if (!X) throw Err(PQDTS_E_ARG, "null X");
+    pqdts::get_x_colmajor(*c, X);
+  });
+}
+
+int pqdts_cuda_set_space(pqdts_ctx* c, int32_t fullspace, const int32_t* maxr) {
+  return guarded(c, [&] {
+    pqdts::need_problem(*c);
+    if (fullspace) {
+      c->fullspace = true;
+      if (maxr) CK(cudaMemcpyAsync(c->maxr.p, maxr, c->h.M * 4, cudaMemcpyHostToDevice, c->st));
+    } else {
+      if (!maxr) throw Err(PQDTS_E_ARG, "reduced space needs maxr");
+      for (int64_t j = 0; j < c->h.M; ++j)
+        if (maxr[j] < 0 || maxr[j] >= c->h.N) throw Err(PQDTS_E_ARG, "maxr out of range");
+      CK(cudaMemcpyAsync(c->maxr.p, maxr, c->h.M * 4, cudaMemcpyHostToDevice, c->st));
+      c->fullspace = false;
+    }
+    CK(cudaStreamSynchronize(c->st));
+  });
+}
+
+int pqdts_cuda_get_maxr(pqdts_ctx* c, int32_t* maxr) {
+  return guarded(c, [&] {
+    pqdts::need_problem(*c);
+    CK(cudaMemcpyAsync(maxr, c->maxr.p, c->h.M * 4, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  });
+}
+
+int pqdts_cuda_L(pqdts_ctx* c, double* val) {
+  return guarded(c, [&] {
+    pqdts::need_problem(*c);
+    *val = pqdts::op_L(*c);
+  });
+}
+
+int pqdts_cuda_dL(pqdts_ctx* c, double* G) {
+  return guarded(c, [&] {
+    pqdts::need_problem(*c);
+    pqdts::op_dL(*c, c->X.p, c->G.p);
+    pqdts::download_rowmajor_to_col(*c, c->G.p, G);
+  });
+}
+
+int pqdts_cuda_redO(pqdts_ctx* c, double* O) {
+  return guarded(c, [&] {
+    pqdts::need_problem(*c);
+    const int N = (int)c->h.N, D = (int)c->h.D;
+    pqdts::DevBands bd = pqdts::bands_of(*c);
+    // R = 2*O - 0 via the Hessian epilogue, halved on the host (exact).
+    pqdts::k_fwd<double, 1><<<dim3(pqdts::cdiv(N, pqdts::kBX), pqdts::cdiv(D, pqdts::kBY), 1),
+                              dim3(pqdts::kBX, pqdts::kBY), 0, c->st>>>(bd, c->fval.p, c->X.p, 0, nullptr, c->R.p,
+                                                                        nullptr, nullptr);
+    pqdts::post_launch(*c);
+    CK(cudaMemcpyAsync(O, c->R.p, (size_t)D * N * 8, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (size_t k = 0; k < (size_t)D * N; ++k) O[k] *= 0.5;
+  });
+}
+
+int pqdts_cuda_BF(pqdts_ctx* c, const double* V, double* HV) {
+  return guarded(c, [&] {
+    pqdts::need_problem(*c);
+    const int64_t M = c->h.M, N = c->h.N;
+    std::vector<double> rm((size_t)M * N);
+    for (int64_t i = 0; i < M; ++i)
+      for (int64_t n = 0; n < N; ++n) rm[(size_t)i * N + n] = V[i + n * M];
+    auto& b = c->cg64;
+    CK(cudaMemcpyAsync(b.p.p, rm.data(), rm.size() * 8, cudaMemcpyHostToDevice, c->st));
+    if (!c->fullspace) {
+      pqdts::k_cg_lift<double><<<pqdts::cdiv(M, pqdts::kRowThreads), pqdts::kRowThreads, 0, c->st>>>(
+          nullptr, 0, (int)M, (int)N, b.p.p, b.z.p, c->maxr.p, b.V.p, b.rs.p);
+      pqdts::post_launch(*c);
+    }
+    pqdts::hvp<double>(*c, b, c->fval.p, c->tval.p, nullptr, false);
+    pqdts::download_rowmajor_to_col(*c, b.Hp.p, HV);
+  });
+}
+
+int pqdts_cuda_Bdiag(pqdts_ctx* c, double* BD) {
+  return guarded(c, [&] {
+    pqdts::need_problem(*c);
+    const int64_t M = c->h.M, N = c->h.N;
+    const double f = c->fullspace ? 1.0 : 2.0;
+    for (int64_t n = 0; n < N; ++n)
+      for (int64_t i = 0; i < M; ++i) BD[i + n * M] = c->h.bdiag[i] * f;
+  });
+}
+
+int pqdts_cuda_doproj(pqdts_ctx* c) {
+  return guarded(c, [&] {
+    pqdts::need_problem(*c);
+    const int M = (int)c->h.M, N = (int)c->h.N;
+    pqdts::k_simplex<<<dim3(pqdts::cdiv((int64_t)M * 32, 128), 1), 128, 0, c->st>>>(c->X.p, nullptr, nullptr, c->X.p,
+                                                                                     (int64_t)M * N, M, N);
+    pqdts::post_launch(*c);
+    CK(cudaStreamSynchronize(c->st));
+  });
+}
+
+int pqdts_cuda_doproj2(pqdts_ctx* c, double* xmin) {
+  return guarded(c, [&] {
+    pqdts::need_problem(*c);
+    const int M = (int)c->h.M, N = (int)c->h.N;
+    const int gb = pqdts::cdiv(M, pqdts::kRowThreads);
+    pqdts::k_cand_proj2<<<dim3(gb, 1), pqdts::kRowThreads, 0, c->st>>>(c->X.p, nullptr, nullptr, c->X.p,
+                                                                         (int64_t)M * N, c->maxr.p, M, N, 0,
+                                                                         c->part2.p);
+    pqdts::post_launch(*c);
+    pqdts::reduce_to(*c, c->part2.p, gb, c->sc.p + pqdts::SC_TMP, 1, true, 0.0);
+    pqdts::read_back(*c, c->sc.p + pqdts::SC_TMP, 1);
+    if (xmin) *xmin = c->pin[0];
+  });
+}
+
+int pqdts_cuda_conv_test(pqdts_ctx* c, double* conv) {
+  return guarded(c, [&] {
+    pqdts::need_problem(*c);
+    *conv = pqdts::op_conv(*c, false);
+  });
+}
+
+int pqdts_cuda_simplexproj(pqdts_ctx* c, const double* y, double* x, int64_t len, int64_t rows) {
+  return guarded(c, [&] {
+    if (!y || !x || len <= 0 || rows <= 0) throw Err(PQDTS_E_ARG, "bad simplexproj arguments");
+    if (len * rows >= ((int64_t)1 << 31)) throw Err(PQDTS_E_ARG, "simplexproj input too large");
+    pqdts::DBuf<double> d;
+    d.alloc((size_t)(len * rows));
+    CK(cudaMemcpyAsync(d.p, y, len * rows * 8, cudaMemcpyHostToDevice, c->st));
+    pqdts::k_simplex<<<dim3(pqdts::cdiv(rows * 32, 128), 1), 128, 0, c->st>>>(d.p, nullptr, nullptr, d.p, 0,
+                                                                                (int)rows, (int)len);
+    pqdts::post_launch(*c);
+    CK(cudaMemcpyAsync(x, d.p, len * rows * 8, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  });
+}
+
+int pqdts_cuda_run_stage(pqdts_ctx* c, int32_t mode, int32_t oiter, int32_t maxiiter, double conv_thres,
+                         int32_t output, double* stats) {
+  return guarded(c, [&] {
+    pqdts::need_problem(*c);
+    if (mode != 1 && mode != 2) throw Err(PQDTS_E_ARG, "mode must be 1 or 2");
+    if (oiter != 1 && oiter != 2) throw Err(PQDTS_E_ARG, "oiter must be 1 or 2");
+    pqdts::SolveState st;
+    c->n_cg = c->n_lsL = c->n_refine = 0;
+    const double t0 = pqdts::wall();
+    st.t0 = t0;
+    pqdts::run_stage(*c, mode, oiter, maxiiter, conv_thres, output, st);
+    CK(cudaStreamSynchronize(c->st));
+    pqdts::fill_stats(*c, st, pqdts::wall() - t0, stats);
+  });
+}
+
+int pqdts_cuda_solve(pqdts_ctx* c, int32_t mode, int32_t maxiiter, double conv_thres, int32_t start_stage,
+                     int32_t output, pqdts_stage_cb cb, void* user, double* stats) {
+  return guarded(c, [&] { pqdts::solve(*c, mode, maxiiter, conv_thres, start_stage, output, cb, user, stats); });
+}
+
+int pqdts_cuda_timer(pqdts_ctx* c, const char* name, double* seconds, int64_t* count) {
+  return guarded(c, [&] {
+    c->timers.flush();
+    for (size_t i = 0; i < c->timers.names.size(); ++i)
+      if (c->timers.names[i] == name) {
+        if (seconds) *seconds = c->timers.secs[i];
+        if (count) *count = c->timers.counts[i];
+        return;
+      }
+    if (seconds) *seconds = 0;
+    if (count) *count = 0;
+  });
+}
+
+int pqdts_cuda_solve_batch(int32_t device, int32_t n_inst, const int64_t* M, const int64_t* N, const int64_t* D,
+                           const int64_t* band_lo, const int64_t* band_hi, const double* band_vals,
+                           const int64_t* band_row_offset, const int64_t* band_val_offset, const double* P,
+                           const int64_t* P_offset, const double* gamma, int32_t precision, int32_t mode,
+                           int32_t maxiiter, double conv_thres, double* X, double* stats) {
+  if (n_inst <= 0 || !M || !N || !D || !band_lo || !band_hi || !band_vals || !band_row_offset || !band_val_offset ||
+      !P || !P_offset || !gamma || !X)
+    return PQDTS_E_ARG;
+  // Instances are independent: a pool of host workers, each with its own
+  // context and stream, so the instances' kernels overlap on the device.
+  std::vector<int64_t> xoff(n_inst + 1, 0);
+  for (int k = 0; k < n_inst; ++k) xoff[k + 1] = xoff[k] + M[k] * N[k];
+  const int workers = std::min<int>(n_inst, 8);
+  std::atomic<int> next{0};
+  std::atomic<int> rc{PQDTS_OK};
+  std::mutex err_mu;
+  auto work = [&]() {
+    pqdts_ctx* c = nullptr;
+    int r = pqdts_cuda_create(device, &c);
+    if (r != PQDTS_OK) {
+      rc = r;
+      return;
+    }
+    for (;;) {
+      const int k = next++;
+      if (k >= n_inst || rc.load() != PQDTS_OK) break;
+      const int64_t* lo = band_lo + band_row_offset[k];
+      const int64_t* hi = band_hi + band_row_offset[k];
+      r = pqdts_cuda_set_problem(c, M[k], N[k], D[k], lo, hi, band_vals + band_val_offset[k], P + P_offset[k],
+                                 gamma[k], precision);
+      if (r == PQDTS_OK) r = pqdts_cuda_set_x(c, X + xoff[k]);
+      if (r == PQDTS_OK)
+        r = pqdts_cuda_solve(c, mode, maxiiter, conv_thres, 1, 0, nullptr, nullptr,
+                             stats ? stats + (int64_t)k * PQDTS_NSTATS : nullptr);
+      if (r == PQDTS_OK) r = pqdts_cuda_get_x(c, X + xoff[k]);
+      if (r != PQDTS_OK) {
+        std::lock_guard<std::mutex> g(err_mu);
+        fprintf(stderr, "pqdts_cuda_solve_batch: instance %d: %s\n", k, c->err.c_str());
+        rc = r;
+      }
+    }
+    pqdts_cuda_destroy(c);
+  };
+  std::vector<std::thread> th;
+  for (int w = 0; w < workers; ++w) th.emplace_back(work);
+  for (auto& t : th) t.join();
+  return rc.load();
+}
+
+}  // extern "C"

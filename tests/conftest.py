@@ -1,0 +1,36 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session")
+def built():
+    """Build the CUDA library, the CLI and the oracle once per session."""
+    import __graft_entry__
+
+    __graft_entry__.build()
+    return True
+
+
+@pytest.fixture(scope="session")
+def cfg1():
+    from pqdts_gb300 import synth
+
+    return synth.make_config(1, seed=0)
+
+
+@pytest.fixture(scope="session")
+def small():
+    """A small banded instance with a nontrivial active set and gamma."""
+    from pqdts_gb300 import synth
+
+    return synth.make_instance(M=80, N=12, D=160, xmax=60.0, eta=0.85, shots=10**5, gamma=1e-3, eps=1e-6, seed=7)

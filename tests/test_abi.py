@@ -1,0 +1,55 @@
+"""The C-ABI library loads on a machine without a GPU and exports every
+symbol that include/pqdts_cuda.h declares; without a device the entry points
+return error codes instead of crashing or falling back to the CPU."""
+import ctypes as C
+import os
+import re
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = []
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if f.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", f)).read()
+            names += re.findall(r"^\s*int\s+(pqdts_cuda_\w+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    for must in ("pqdts_cuda_create", "pqdts_cuda_set_problem", "pqdts_cuda_solve", "pqdts_cuda_L", "pqdts_cuda_dL",
+                 "pqdts_cuda_BF", "pqdts_cuda_simplexproj", "pqdts_cuda_solve_batch"):
+        assert must in names
+
+
+def test_library_exports_all_declared_symbols(built):
+    import pqdts_gb300 as pq
+
+    L = C.CDLL(pq.LIB_PATH)
+    missing = [n for n in _declared() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_no_device_is_an_error_code(built):
+    import torch
+
+    if torch.cuda.is_available():
+        import pytest
+
+        pytest.skip("a GPU is present")
+    import pqdts_gb300 as pq
+
+    h = C.c_void_p()
+    rc = pq.lib().pqdts_cuda_create(0, C.byref(h))
+    assert rc < 0 and not h.value
+
+
+def test_cli_usage_without_args(built):
+    import subprocess
+
+    import pqdts_gb300 as pq
+
+    r = subprocess.run([pq.CLI_PATH], capture_output=True, text=True)
+    assert r.returncode == 1 and "usage" in r.stderr

@@ -1,0 +1,188 @@
+"""Per-operation parity of the CUDA path (through the C ABI) against the oracle.
+
+The banded products accumulate in the reference's order with one fma per
+term on both sides, so redO, dL, BF, Bdiag and doproj2 must be bit-identical.
+L and conv_test end in tree reductions on the GPU (sequential chains in the
+oracle): relative tolerance 1e-13.  doproj uses a different exact-threshold
+algorithm than Condat's (same projection): absolute tolerance 1e-14.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+REL_REDUCTION = 1e-13
+ABS_PROJECTION = 1e-14
+
+
+def _pair(inst, precision=0):
+    import pqdts_gb300 as pq
+    from oracle.oracle import Oracle
+
+    s = pq.Solver(0)
+    s.set_instance(inst, precision)
+    return s, Oracle.from_instance(inst)
+
+
+def _random_x(inst, seed, feasible=True):
+    rng = np.random.default_rng(seed)
+    X = rng.random((inst.M, inst.N))
+    if feasible:
+        X /= X.sum(axis=1, keepdims=True)
+        X[rng.random(X.shape) < 0.2] = 0.0
+        X /= np.maximum(X.sum(axis=1, keepdims=True), 1e-300)
+    return np.asfortranarray(X)
+
+
+def _maxr(X):
+    return np.argmax(X, axis=1).astype(np.int32)
+
+
+@pytest.mark.parametrize("which", ["cfg1", "small"])
+def test_bands_and_bdiag(built, request, which):
+    inst = request.getfixturevalue(which)
+    s, o = _pair(inst)
+    lo, hi, nnz = s.bands()
+    olo, ohi, _, oval = o.bands()
+    assert np.array_equal(lo, olo) and np.array_equal(hi, ohi) and nnz == oval.size
+    for full in (True, False):
+        m = None if full else _maxr(_random_x(inst, 1))
+        s.set_space(full, m)
+        o.set_space(full, m)
+        assert np.array_equal(s.Bdiag(), o.Bdiag())
+
+
+@pytest.mark.parametrize("which", ["cfg1", "small"])
+def test_redO_bitwise(built, request, which):
+    inst = request.getfixturevalue(which)
+    s, o = _pair(inst)
+    X = _random_x(inst, 2)
+    s.set_x(X)
+    assert np.array_equal(s.redO(), o.redO(X))
+
+
+@pytest.mark.parametrize("which", ["cfg1", "small"])
+@pytest.mark.parametrize("full", [True, False])
+def test_L_dL(built, request, which, full):
+    inst = request.getfixturevalue(which)
+    s, o = _pair(inst)
+    X = _random_x(inst, 3)
+    m = None if full else _maxr(X)
+    s.set_space(full, m)
+    o.set_space(full, m)
+    s.set_x(X)
+    Lg = s.L()
+    Lo, Xo = o.L(X)
+    assert abs(Lg - Lo) <= REL_REDUCTION * abs(Lo)
+    assert np.array_equal(s.get_x(), Xo)  # reduced space: identical max-column rebuild
+    s.set_x(X)
+    G = s.dL()
+    Go, Xo2 = o.dL(X)
+    assert np.array_equal(G, Go)
+    assert np.array_equal(s.get_x(), Xo2)
+
+
+@pytest.mark.parametrize("which", ["cfg1", "small"])
+@pytest.mark.parametrize("full", [True, False])
+def test_BF_bitwise(built, request, which, full):
+    inst = request.getfixturevalue(which)
+    s, o = _pair(inst)
+    X = _random_x(inst, 4)
+    m = None if full else _maxr(X)
+    s.set_space(full, m)
+    o.set_space(full, m)
+    V = np.asfortranarray(np.random.default_rng(5).standard_normal((inst.M, inst.N)))
+    assert np.array_equal(s.BF(V), o.BF(V))
+
+
+@pytest.mark.parametrize("which", ["cfg1", "small"])
+def test_doproj(built, request, which):
+    inst = request.getfixturevalue(which)
+    s, o = _pair(inst)
+    Y = np.asfortranarray(np.random.default_rng(6).standard_normal((inst.M, inst.N)) * 0.7 + 0.05)
+    s.set_x(Y)
+    s.doproj()
+    Xg = s.get_x()
+    Xo = o.doproj(Y)
+    assert np.max(np.abs(Xg - Xo)) <= ABS_PROJECTION
+    assert Xg.min() >= 0.0
+    assert np.max(np.abs(Xg.sum(axis=1) - 1.0)) < 1e-13
+    # zero pattern identical away from the threshold
+    assert np.array_equal(Xg > 1e-12, Xo > 1e-12)
+
+
+@pytest.mark.parametrize("which", ["cfg1", "small"])
+def test_doproj2_bitwise(built, request, which):
+    inst = request.getfixturevalue(which)
+    s, o = _pair(inst)
+    X = _random_x(inst, 7)
+    Y = np.asfortranarray(X + 0.01 * np.random.default_rng(8).standard_normal(X.shape))
+    m = _maxr(X)
+    s.set_space(False, m)
+    o.set_space(False, m)
+    s.set_x(Y)
+    xmin = s.doproj2()
+    Xo, xmino = o.doproj2(Y)
+    assert np.array_equal(s.get_x(), Xo)
+    assert xmin == xmino
+
+
+@pytest.mark.parametrize("which", ["cfg1", "small"])
+@pytest.mark.parametrize("full", [True, False])
+def test_conv_test(built, request, which, full):
+    inst = request.getfixturevalue(which)
+    s, o = _pair(inst)
+    X = _random_x(inst, 9)
+    m = None if full else _maxr(X)
+    s.set_space(full, m)
+    o.set_space(full, m)
+    s.set_x(X)
+    cg = s.conv_test()
+    co, Xo, _ = o.conv_test(X)
+    assert abs(cg - co) <= REL_REDUCTION * abs(co)
+    assert np.array_equal(s.get_x(), Xo)
+
+
+def test_simplexproj_dropin(built):
+    """pqdts_cuda_simplexproj is the drop-in for simplexproj_condat_."""
+    import pqdts_gb300 as pq
+    from oracle.oracle import condat
+
+    rng = np.random.default_rng(10)
+    with pq.Solver(0) as s:
+        for n in (1, 2, 3, 31, 32, 33, 200, 1000):
+            Y = rng.standard_normal((5, n)) * rng.choice([1e-3, 1.0, 50.0])
+            Xg = s.simplexproj(Y)
+            Xo = np.stack([condat(y) for y in Y])
+            assert np.max(np.abs(Xg - Xo)) <= 1e-14 * max(1.0, np.abs(Y).max())
+            assert Xg.min() >= 0 and np.max(np.abs(Xg.sum(1) - 1)) < 1e-12
+
+
+def test_internal_F(built):
+    """F computed internally (nnzF < 0, M == (D-1)^2), random P from the seeded stream."""
+    import pqdts_gb300 as pq
+    from oracle.oracle import Oracle
+
+    M, N, D = 400, 20, 21
+    with pq.Solver(0) as s:
+        s.set_problem_coo(M, N, D, None, None, 1e-4)
+        o = Oracle(M, N, D, 1e-4, None, None)
+        lo, hi, nnz = s.bands()
+        olo, ohi, _, oval = o.bands()
+        assert np.array_equal(lo, olo) and np.array_equal(hi, ohi) and nnz == oval.size
+        X = _random_x(type("I", (), {"M": M, "N": N})(), 11)
+        s.set_x(X)
+        assert np.array_equal(s.dL(), o.dL(X)[0])
+        assert np.array_equal(s.maxr(), o.maxr())
+
+
+def test_errors_are_codes(built):
+    import pqdts_gb300 as pq
+
+    with pq.Solver(0) as s:
+        with pytest.raises(pq.PqdtsError, match="no problem set"):
+            s.L()
+        with pytest.raises(pq.PqdtsError, match="out of range"):
+            s.set_problem_coo(10, 3, 5, (np.array([0]), np.array([99]), np.array([1.0])), None, 0.0)
+        with pytest.raises(pq.PqdtsError, match=r"\(D-1\)"):
+            s.set_problem_coo(10, 3, 5, None, None, 0.0)
