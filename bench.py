@@ -1,0 +1,452 @@
+#!/usr/bin/env python3
+"""Benchmark: time-to-solution of pqdts's two-metric projected truncated
+Newton solve (mode 2, two stages, start Pi = 1/N) on one GB300.
+
+Workload: the M=2000, N=200, D=4000 configuration (x_d linear 0.01..1800,
+eta = 0.9, 1e7 shots, gamma = 1e-5), seeded synthetic data (pqdts_gb300.synth),
+solved to conv < 1e-9 -- the tolerance at which the final objective is pinned
+to ~1e-12 relative, so each step is a solve to 1e-8 relative objective
+(verified against an FP64 solve to conv < 1e-10 made before timing).
+
+One "step" = one full solve.  `value` = seconds per solve with the problem
+resident in HBM (CUDA events on the library's stream); `e2e` = the same
+through the C ABI with host buffers (problem upload, starting point upload,
+solve, result download inside the timed region).  The FP64 path is the
+drop-in (bitwise the oracle's trajectory); the mixed-precision solver on the
+same inputs is reported beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
+  python bench.py --impl reference ...   # the CPU restatement on host cores
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+CONFIG = 2
+EPS = 1e-9
+EPS_REF = 1e-10
+# Full-solve work of the default workload (FP64 trajectory, identical for the
+# GPU path and the CPU restatement): outer iterations, CG iterations,
+# line-search objective evaluations.  Used to scale the CPU samples.
+FULL_SOLVE_WORK = None
+
+
+def _passes(outer, cg, ls):
+    """Banded-product passes (one pass = nnz*N FMAs) of a mode-2 solve:
+    per outer iteration dL + dL after CG + L + dL + conv_test's dL (9 passes),
+    2 per CG iteration (BF), 1 per line-search objective."""
+    return 2.0 * cg + 9.0 * outer + ls
+
+
+# --------------------------------------------------------------------------
+# clocks during the timed region
+# --------------------------------------------------------------------------
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# --------------------------------------------------------------------------
+# CPU restatement (oracle) sample, run in a clean subprocess so OpenMP sees
+# the binding environment of pqdts.py (OMP_PROC_BIND, OMP_PLACES).
+# --------------------------------------------------------------------------
+def cpu_sample(config, seed, maxiter, eps, threads):
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads), OMP_PROC_BIND="true", OMP_PLACES="cores")
+    code = (
+        "import json,sys; sys.path.insert(0,%r)\n"
+        "from pqdts_gb300 import synth\n"
+        "from oracle.oracle import Oracle, set_threads\n"
+        "set_threads(%d)\n"
+        "inst=synth.make_config(%d, seed=%d)\n"
+        "o=Oracle.from_instance(inst)\n"
+        "X,st=o.solve(mode=2,maxiter=%d,eps=%r)\n"
+        "print(json.dumps(st))\n" % (ROOT, threads, config, seed, maxiter, eps))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env)
+    if r.returncode != 0:
+        raise RuntimeError("oracle sample failed: " + r.stderr[-2000:])
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline_value(st_full, config, seed, eps, sample_iters):
+    cores = host_cores()
+    st = cpu_sample(config, seed, sample_iters, eps, cores)
+    work_s = _passes(st["outer"], st["cg"], st["ls"])
+    work_f = _passes(st_full["outer"], st_full["cg"], st_full["ls_evals"])
+    value = st["seconds"] * work_f / work_s
+    return {"value": value, "unit": "s", "cores": cores, "kind": "port",
+            "sample": (f"oracle (C++/OpenMP restatement) on the first {sample_iters} outer iterations of each stage "
+                       f"({int(st['outer'])} outer, {int(st['cg'])} CG, {int(st['ls'])} line-search evaluations, "
+                       f"{st['seconds']:.2f} s), scaled by banded-product passes to the full solve "
+                       f"({work_f:.0f} / {work_s:.0f} passes)")}
+
+
+# --------------------------------------------------------------------------
+# distributed helpers (one process per GPU; independent instances per rank)
+# --------------------------------------------------------------------------
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def dist_init(world, use_cuda):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("nccl" if use_cuda else "gloo")
+    return dist
+
+
+def dist_max(dist, v, device):
+    if dist is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# --------------------------------------------------------------------------
+# reference arm: the CPU restatement on the host cores
+# --------------------------------------------------------------------------
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    cores = host_cores()
+    samples = []
+    info = None
+    for k in range(args.warmup + args.steps):
+        st = cpu_sample(CONFIG, 0, args.ref_sample_iters, EPS, cores)
+        if k >= args.warmup:
+            samples.append(st)
+        info = st
+    if FULL_SOLVE_WORK is None:
+        work_f = None
+    else:
+        work_f = _passes(*FULL_SOLVE_WORK)
+    per_pass = [s["seconds"] / _passes(s["outer"], s["cg"], s["ls"]) for s in samples]
+    sec_per_pass = statistics.mean(per_pass)
+    value = sec_per_pass * work_f if work_f else None
+    unit = "s" if work_f else "s per banded-product pass"
+    if value is None:
+        value = sec_per_pass
+    line = {
+        "impl": "reference", "metric": "time-to-solution at 1e-8 rel. objective (mode-2 solve, s)", "value": value,
+        "unit": unit, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": statistics.mean(s["seconds"] for s in samples) * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, pqdts_gb300.synth)",
+        "config": {"workload": "M=2000 N=200 D=4000 mode-2 solve to conv<1e-9", "threads": cores},
+        "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "kind": "port",
+                         "sample": f"oracle restatement, first {args.ref_sample_iters} outer iterations per stage, "
+                                   f"scaled by banded-product passes to the full solve"},
+        "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "last_sample": info,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# --------------------------------------------------------------------------
+# our arm
+# --------------------------------------------------------------------------
+def fp64_peak_tflops(device):
+    """cuBLAS DGEMM (torch.matmul float64, n=4096) best of 5: the FP64
+    denominator of the roofline (the banded products are FP64-ALU bound)."""
+    import torch
+
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=device)
+    b = torch.randn(n, n, dtype=torch.float64, device=device)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = math.inf
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1) * 1e-3)
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return json.load(open(path))
+    except (OSError, ValueError):
+        return {}
+
+
+def profile_traffic(name):
+    """dram bytes per launch from a committed ncu summary (profiles/<name>),
+    line `traffic_bytes_per_launch: <int>`; None when absent."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import pqdts_gb300 as pq
+    from pqdts_gb300 import synth
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = dist_init(world, True)
+    prec = pq.MIXED if args.precision == "mixed" else pq.FP64
+    inst = synth.make_config(CONFIG, seed=rank)
+
+    # reference objective of this instance: FP64 solve to conv < 1e-10
+    with pq.Solver(local) as sref:
+        sref.set_instance(inst, pq.FP64)
+        st_ref = sref.solve(mode=2, maxiter=5000, eps=EPS_REF)
+    L_star = st_ref["L"]
+
+    s = pq.Solver(local)
+    s.set_instance(inst, prec)
+    stream = torch.cuda.ExternalStream(s.stream(), device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
+
+    for _ in range(args.warmup):
+        s.init_x()
+        s.solve(mode=2, maxiter=5000, eps=EPS)
+
+    bf0 = s.timer("BF")
+    launches0 = s.kernel_launches()
+    times, stats = [], []
+    clocks = Clocks(local)
+    dist_barrier(dist)
+    torch.cuda.synchronize()
+    clocks.start()
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        flush.fill_(1.0)  # L2 flush between steps (not timed: separate stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.init_x()
+        st = s.solve(mode=2, maxiter=5000, eps=EPS)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+        stats.append(st)
+    torch.cuda.synchronize()
+    dist_barrier(dist)
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    launches = s.kernel_launches() - launches0
+    bf1 = s.timer("BF")
+    step_s = dist_max(dist, statistics.mean(times), dev)
+    rel_err = abs(stats[-1]["L"] - L_star) / abs(L_star)
+    assert rel_err <= 1e-8, f"objective {stats[-1]['L']} not within 1e-8 of {L_star}"
+
+    # roofline of the dominant kernels: the banded products of the CG's
+    # Hessian product (k_fwd + k_trans), FP64- (or FP32-) ALU bound.
+    nnz, N, M, D = inst.nnz, inst.N, inst.M, inst.D
+    cg = sum(x["cg"] for x in stats)
+    bf_time = bf1[0] - bf0[0]
+    flops_pair = 2 * 2.0 * nnz * N
+    achieved_tf = flops_pair * cg / bf_time / 1e12 if bf_time > 0 else None
+    peaks = measured_peaks()
+    if prec == pq.FP64:
+        peak_tf = fp64_peak_tflops(dev)
+        peak_note = "cuBLAS DGEMM (n=4096) measured in this run; FP64 is the binding unit"
+    else:
+        peak_tf = None
+        peak_note = "FP32 CUDA-core products; see profiles/"
+    sval = 8 if prec == pq.FP64 else 4
+    bytes_pass = nnz * (sval + 4) + (D + 1) * 8 + M * N * sval + D * N * sval
+    traffic = profile_traffic("spmm_fp64_config2.txt" if prec == pq.FP64 else "spmm_fp32_config2.txt")
+    roofline = {
+        "kernel": "k_fwd + k_trans (Hessian product: O = F.V, F^T.(2O) + stencil)",
+        "bound": "fp64" if prec == pq.FP64 else "fp32",
+        "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
+        "frac": (achieved_tf / peak_tf) if (achieved_tf and peak_tf) else None,
+        "peak_source": peak_note,
+        "traffic": traffic,
+        "algorithmic_flops_per_launch": flops_pair / 2,
+        "algorithmic_bytes_per_launch": bytes_pass,
+        "hbm_view": {"achieved": bytes_pass * 2 * cg / bf_time / 1e9 if bf_time > 0 else None,
+                     "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": (bytes_pass * 2 * cg / bf_time / 1e9 / peaks["hbm_gbs"]) if (bf_time > 0 and
+                                                                                        peaks.get("hbm_gbs")) else None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+    }
+
+    # e2e through the C ABI with host buffers
+    e2e_times = []
+    h2d = d2h = 0
+    X0 = np.full((inst.M, inst.N), 1.0 / inst.N, order="F")
+    for _ in range(max(1, args.steps)):
+        torch.cuda.synchronize()
+        with pq.Solver(local) as se:
+            a0 = se.transfer_bytes()
+            t0 = time.perf_counter()
+            se.set_instance(inst, prec)
+            se.set_x(X0)
+            se.solve(mode=2, maxiter=5000, eps=EPS)
+            Xe = se.get_x()
+            e2e_times.append(time.perf_counter() - t0)
+            a1 = se.transfer_bytes()
+            h2d, d2h = a1[0] - a0[0], a1[1] - a0[1]
+    e2e_s = dist_max(dist, statistics.mean(e2e_times), dev)
+
+    # mixed precision on the same inputs (reported beside the FP64 drop-in)
+    extra = {}
+    if prec == pq.FP64 and args.with_mixed and world == 1:
+        with pq.Solver(local) as sm:
+            sm.set_instance(inst, pq.MIXED)
+            stream_m = torch.cuda.ExternalStream(sm.stream(), device=dev)
+            for _ in range(args.warmup):
+                sm.init_x()
+                sm.solve(mode=2, maxiter=5000, eps=EPS)
+            mt, ms = [], []
+            for _ in range(args.steps):
+                flush.fill_(1.0)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream_m)
+                sm.init_x()
+                stm = sm.solve(mode=2, maxiter=5000, eps=EPS)
+                e1.record(stream_m)
+                e1.synchronize()
+                mt.append(e0.elapsed_time(e1) * 1e-3)
+                ms.append(stm)
+            mval = statistics.mean(mt)
+            extra["mixed"] = {"value": mval, "unit": "s", "speedup_vs_fp64": step_s / mval,
+                              "rel_obj_err_vs_fp64_ref": abs(ms[-1]["L"] - L_star) / abs(L_star),
+                              "outer": ms[-1]["outer"], "cg": ms[-1]["cg"], "refine": ms[-1]["refine"]}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline_value(stats[-1], CONFIG, rank, EPS, args.cpu_sample_iters)
+        except Exception as e:  # reported, never silently replaced
+            cpu = {"value": None, "error": str(e)[:300]}
+
+    if rank == 0:
+        line = {
+            "metric": "time-to-solution at 1e-8 rel. objective (mode-2 solve, s)",
+            "value": step_s, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": step_s * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == pq.FP64 else "f32+f64",
+            "data": "synthetic (seeded, pqdts_gb300.synth; rank r uses seed r)",
+            "config": {"workload": "M=2000 N=200 D=4000 x_max=1800 eta=0.9 shots=1e7 gamma=1e-5, "
+                                   "mode-2 two-stage solve from Pi=1/N to conv<1e-9",
+                       "nnz_F": nnz, "precision": args.precision, "l2": "flushed between steps (256 MiB write)",
+                       "objective": stats[-1]["L"], "objective_ref_fp64_1e-10": L_star,
+                       "rel_obj_err": rel_err, "outer": stats[-1]["outer"], "cg": stats[-1]["cg"],
+                       "ls_evals": stats[-1]["ls_evals"], "parallelism": f"{world} independent instance(s)"},
+            "solves_per_s": world / step_s,
+            "wall_s_timed_region": t_wall,
+            "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        line.update(extra)
+        print(json.dumps(line))
+    s.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--with-mixed", dest="with_mixed", action="store_true", default=True)
+    ap.add_argument("--no-mixed", dest="with_mixed", action="store_false")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-iters", type=int, default=2)
+    ap.add_argument("--ref-sample-iters", type=int, default=1)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

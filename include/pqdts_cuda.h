@@ -77,6 +77,13 @@ int pqdts_cuda_get_bands(pqdts_ctx* ctx, int64_t* band_lo, int64_t* band_hi, int
 /* Current iterate X (M,N) column-major (pqdts.f90:1834-1838, 1874). */
 int pqdts_cuda_set_x(pqdts_ctx* ctx, const double* X_colmajor);
 int pqdts_cuda_get_x(pqdts_ctx* ctx, double* X_colmajor);
+/* X = 1/N on the device, the reference's starting point (pqdts.f90:1834-1838). */
+int pqdts_cuda_init_x(pqdts_ctx* ctx);
+
+/* The context's CUDA stream (cudaStream_t) for event timing by the caller. */
+int pqdts_cuda_get_stream(pqdts_ctx* ctx, void** stream);
+/* Bytes this context has copied host->device and device->host so far. */
+int pqdts_cuda_transfer_bytes(pqdts_ctx* ctx, int64_t* h2d, int64_t* d2h);
 
 /* Space of the per-operation entry points below: fullspace = 1 is the
  * reference's tfullspace = .true.; otherwise maxr (M entries, 0-based) is

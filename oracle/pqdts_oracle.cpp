@@ -17,11 +17,15 @@
 //     (tests/test_oracle_derivatives.py).
 //
 // Arithmetic conventions (what makes this restatement deterministic):
-//   * Reductions follow the reference's single-thread order (OMP_NUM_THREADS
-//     = 1): every Fortran SUM(...) is a left-to-right chain, every OpenMP
-//     reduction is "0 + (chain over the loop)" added to the incoming value.
-//     OpenMP is used here only over independent outputs, so the result does
-//     not depend on the thread count.
+//   * Reductions follow one fixed order of the reference: every Fortran
+//     SUM(...) is a left-to-right chain; every OpenMP reduction is evaluated
+//     as if each loop iteration ran on its own thread and the private sums
+//     were combined in ascending order.  For pdot, L's residual sum and
+//     conv_test this equals the single-thread order; for L's gamma term it
+//     is the order of one thread per column (the reference's own value of
+//     that term depends on OMP_NUM_THREADS).  OpenMP is used here only over
+//     independent outputs, so the result does not depend on the thread
+//     count.
 //   * a + b*c in the Fortran source is evaluated as fma(b, c, a), the
 //     contraction GCC applies under -O3 on FMA hardware; b*c + d*e keeps
 //     the first product fused: fma(b, c, round(d*e)).
@@ -336,16 +340,24 @@ struct Oracle {
       if (flo[d] >= 0) red = red + rowsum[d];
     double val = 0.0 + red;
     if (gam != 0) {
-      // L_gam (956-962): one chain over columns, then rows 1..M-1.
-      double g = 0.0;
+      // L_gam (956-962): `val = val + gam*(X(j,i)-X(j+1,i))**2` under
+      // reduction(+:val) schedule(static,1) over columns i.  The reference's
+      // result depends on OMP_NUM_THREADS here (the private accumulator of a
+      // thread spans all its columns).  The oracle fixes the order of one
+      // thread per column: a chain over rows per column, the columns' sums
+      // then added to val in ascending column order.
+      std::vector<double> colsum(N, 0.0);
+#pragma omp parallel for schedule(static)
       for (int64_t n = 0; n < N; ++n) {
         const double* xc = X + n * M;
+        double g = 0.0;
         for (int64_t j = 0; j + 1 < M; ++j) {
           double dx = xc[j] - xc[j + 1];
           g = std::fma(gam, dx * dx, g);
         }
+        colsum[n] = g;
       }
-      val = val + g;
+      for (int64_t n = 0; n < N; ++n) val = val + colsum[n];
     }
     t.stop("L");
     return val;

@@ -54,6 +54,9 @@ def lib():
         "pqdts_cuda_set_problem_coo": [p, i64, i64, i64, i64, p, p, p, i64, p, p, p, d, i32],
         "pqdts_cuda_get_bands": [p, p, p, C.POINTER(i64)],
         "pqdts_cuda_set_x": [p, p],
+        "pqdts_cuda_init_x": [p],
+        "pqdts_cuda_get_stream": [p, C.POINTER(C.c_void_p)],
+        "pqdts_cuda_transfer_bytes": [p, C.POINTER(i64), C.POINTER(i64)],
         "pqdts_cuda_get_x": [p, p],
         "pqdts_cuda_set_space": [p, i32, p],
         "pqdts_cuda_get_maxr": [p, p],
@@ -165,6 +168,21 @@ class Solver:
         X = np.asfortranarray(X, np.float64)
         assert X.shape == (self.M, self.N)
         self._check(self._L.pqdts_cuda_set_x(self.h, _ptr(X)), "set_x")
+
+    def init_x(self):
+        """X = 1/N on the device (the reference's starting point)."""
+        self._check(self._L.pqdts_cuda_init_x(self.h), "init_x")
+
+    def stream(self):
+        """The context's cudaStream_t as an integer handle."""
+        v = C.c_void_p()
+        self._check(self._L.pqdts_cuda_get_stream(self.h, C.byref(v)), "get_stream")
+        return v.value or 0
+
+    def transfer_bytes(self):
+        a, b = C.c_int64(), C.c_int64()
+        self._check(self._L.pqdts_cuda_transfer_bytes(self.h, C.byref(a), C.byref(b)), "transfer_bytes")
+        return a.value, b.value
 
     def get_x(self):
         X = np.empty((self.M, self.N), order="F")

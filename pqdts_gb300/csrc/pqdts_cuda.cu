@@ -21,6 +21,7 @@
 #include <stdexcept>
 #include <string>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/pqdts_cuda.h"
@@ -74,9 +75,10 @@ struct DBuf {
     CK(cudaMalloc((void**)&p, count * sizeof(T)));
     n = count;
   }
-  void upload(const T* h, size_t count, cudaStream_t s) {
+  void upload(const T* h, size_t count, cudaStream_t s, std::atomic<int64_t>* bytes) {
     alloc(count);
     if (count) CK(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    if (bytes) *bytes += (int64_t)(count * sizeof(T));
   }
 };
 
@@ -175,6 +177,7 @@ struct pqdts_ctx {
   std::string err;
   int verbose = 0;
   std::atomic<int64_t> launches{0};
+  std::atomic<int64_t> h2d{0}, d2h{0};
   pqdts::HostProblem h;
   int precision = PQDTS_FP64;
   bool have_problem = false;
@@ -190,6 +193,10 @@ struct pqdts_ctx {
   pqdts::CGBufs<double> cg64;
   pqdts::CGBufs<float> cg32;
   pqdts::DBuf<double> part, part2, sc, alphas, lsout, cglog;
+  // reference-order reductions (FP64 path): residual stack, Condat scratch,
+  // per-row / per-column chain results
+  pqdts::DBuf<double> Rst, aux, srow, gcol, colbuf, lred;
+  bool exact = true;  // FP64: every reduction in the oracle's order
   pqdts::DBuf<int> ipart;
   pqdts::DBuf<long long> icount;
   double* pin = nullptr;  // pinned host scalars
@@ -244,26 +251,38 @@ static void read_back(Ctx& c, const double* dev, int count) {
 static void setup_device(Ctx& c) {
   HostProblem& h = c.h;
   const int64_t M = h.M, N = h.N, D = h.D, MN = M * N;
-  c.flo.upload(h.flo.data(), D, c.st);
-  c.fw.upload(h.fw.data(), D, c.st);
-  c.foff.upload(h.foff.data(), D, c.st);
-  c.fval.upload(h.fval.data(), h.fval.size(), c.st);
-  c.tptr.upload(h.tptr.data(), h.tptr.size(), c.st);
-  c.tidx.upload(h.tidx.data(), h.tidx.size(), c.st);
-  c.tval.upload(h.tval.data(), h.tval.size(), c.st);
-  c.bdiag.upload(h.bdiag.data(), M, c.st);
-  c.P.upload(h.P.data(), h.P.size(), c.st);
+  c.flo.upload(h.flo.data(), D, c.st, &c.h2d);
+  c.fw.upload(h.fw.data(), D, c.st, &c.h2d);
+  c.foff.upload(h.foff.data(), D, c.st, &c.h2d);
+  c.fval.upload(h.fval.data(), h.fval.size(), c.st, &c.h2d);
+  c.tptr.upload(h.tptr.data(), h.tptr.size(), c.st, &c.h2d);
+  c.tidx.upload(h.tidx.data(), h.tidx.size(), c.st, &c.h2d);
+  c.tval.upload(h.tval.data(), h.tval.size(), c.st, &c.h2d);
+  c.bdiag.upload(h.bdiag.data(), M, c.st, &c.h2d);
+  c.P.upload(h.P.data(), h.P.size(), c.st, &c.h2d);
   if (c.precision == PQDTS_MIXED) {
     std::vector<float> f32(h.fval.begin(), h.fval.end());
-    c.fval32.upload(f32.data(), f32.size(), c.st);
+    c.fval32.upload(f32.data(), f32.size(), c.st, &c.h2d);
     std::vector<float> t32(h.tval.begin(), h.tval.end());
-    c.tval32.upload(t32.data(), t32.size(), c.st);
+    c.tval32.upload(t32.data(), t32.size(), c.st, &c.h2d);
     c.cg32.alloc(MN, M, D * N);
   } else {
     c.fval32.release();
     c.tval32.release();
   }
   c.cg64.alloc(MN, M, D * N);
+  c.exact = (c.precision == PQDTS_FP64);
+  if (c.exact) {
+    c.Rst.alloc((size_t)kBatchLS * D * N);
+    c.aux.alloc((size_t)kBatchLS * MN);
+  } else {
+    c.Rst.release();
+    c.aux.release();
+  }
+  c.srow.alloc((size_t)kBatchLS * std::max(D, M));
+  c.gcol.alloc((size_t)kBatchLS * N);
+  c.colbuf.alloc(N);
+  c.lred.alloc(kBatchLS);
   c.X.alloc(MN);
   c.G.alloc(MN);
   c.Xc.alloc((size_t)kBatchLS * MN);
@@ -282,9 +301,10 @@ static void setup_device(Ctx& c) {
   c.lsout.alloc(4 * kBatchLS);
   c.cglog.alloc(4 * kMaxCG);
   // Initial X = 1/N (pqdts.f90:1834-1838) and maxr from the seeded stream.
-  std::vector<double> x0(MN, 1.0 / (double)N);
-  CK(cudaMemcpyAsync(c.X.p, x0.data(), MN * 8, cudaMemcpyHostToDevice, c.st));
+  k_fill<<<elem_grid(MN), 256, 0, c.st>>>(MN, 1.0 / (double)N, c.X.p);
+  post_launch(c);
   CK(cudaMemcpyAsync(c.maxr.p, c.h_maxr.data(), M * 4, cudaMemcpyHostToDevice, c.st));
+  c.h2d += M * 4;
   CK(cudaStreamSynchronize(c.st));
   c.fullspace = true;
   c.have_problem = true;
@@ -303,13 +323,37 @@ static void rebuild(Ctx& c, double* X, int B = 1) {
   post_launch(c);
 }
 
-// Objective of B stacked, already projected/rebuilt matrices -> lsout[b]
-// (L_red) and lsout[kBatchLS + b] (L_gam); values land in c.pin after sync.
+// Objective of B stacked, already projected/rebuilt matrices; the values
+// land in c.pin after fetch_objectives.  FP64 path: O - P is stored and
+// summed in the oracle's order (row chains over n, rows in ascending order,
+// then the gamma term's column chains added column by column).  Mixed path:
+// fixed-shape tree reductions.
 static void objective_stack(Ctx& c, const double* Xs, int B) {
   const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
   DevBands bd = bands_of(c);
   dim3 grid(cdiv(N, kBX), cdiv(D, kBY), B);
-  k_fwd<double, 2><<<grid, dim3(kBX, kBY), 0, c.st>>>(bd, c.fval.p, Xs, (int64_t)M * N, c.P.p, nullptr, c.part.p, nullptr);
+  if (c.exact) {
+    k_fwd<double, 3><<<grid, dim3(kBX, kBY), 0, c.st>>>(bd, c.fval.p, Xs, (int64_t)M * N, c.P.p, c.Rst.p, nullptr,
+                                                        nullptr);
+    post_launch(c);
+    k_rowchain_resid<<<dim3(cdiv(D, kRowThreads), B), kRowThreads, 0, c.st>>>(c.Rst.p, c.flo.p, D, N, c.srow.p);
+    post_launch(c);
+    double* out = c.lsout.p;
+    if (c.h.gam != 0) out = c.lred.p;
+    k_seqsum<<<1, 32, 0, c.st>>>(c.srow.p, D, nullptr, out, B, nullptr);
+    post_launch(c);
+    if (c.h.gam != 0) {
+      k_colchain<1><<<dim3(cdiv(N, 32), B), 256, 0, c.st>>>(Xs, nullptr, (int64_t)M * N, M, N, c.h.gam, c.gcol.p,
+                                                           nullptr);
+      post_launch(c);
+      k_seqsum<<<1, 32, 0, c.st>>>(c.gcol.p, N, c.lred.p, c.lsout.p, B, nullptr);
+      post_launch(c);
+    }
+    CK(cudaMemsetAsync(c.lsout.p + kBatchLS, 0, B * sizeof(double), c.st));
+    return;
+  }
+  k_fwd<double, 2><<<grid, dim3(kBX, kBY), 0, c.st>>>(bd, c.fval.p, Xs, (int64_t)M * N, c.P.p, nullptr, c.part.p,
+                                                      nullptr);
   post_launch(c);
   reduce_to(c, c.part.p, (int64_t)grid.x * grid.y, c.lsout.p, B);
   if (c.h.gam != 0) {
@@ -325,7 +369,7 @@ static void objective_stack(Ctx& c, const double* Xs, int B) {
 static void fetch_objectives(Ctx& c, int B, double* L) {
   CK(cudaMemcpyAsync(c.pin, c.lsout.p, 4 * kBatchLS * sizeof(double), cudaMemcpyDeviceToHost, c.st));
   CK(cudaStreamSynchronize(c.st));
-  for (int b = 0; b < B; ++b) L[b] = c.h.gam != 0 ? c.pin[b] + c.pin[kBatchLS + b] : c.pin[b];
+  for (int b = 0; b < B; ++b) L[b] = (c.h.gam != 0 && !c.exact) ? c.pin[b] + c.pin[kBatchLS + b] : c.pin[b];
 }
 
 // L(X) on the context's X (917-973).
@@ -353,13 +397,22 @@ static void op_dL(Ctx& c, double* X, double* G) {
   post_launch(c);
 }
 
-// sum(a.b) over M*N -> device scalar `out`.
-static void dot_dev(Ctx& c, const double* a, const double* b, double* out) {
-  const int64_t total = c.h.M * c.h.N;
+// pdot (589-614): sum(a.b) over M*N -> device scalar `out`.  FP64 path: one
+// chain per column over the rows, columns added in ascending order.
+static void dot_dev(Ctx& c, const double* a, const double* b, double* out, const double* pred = nullptr) {
+  const int M = (int)c.h.M, N = (int)c.h.N;
+  if (c.exact) {
+    k_colchain<0><<<dim3(cdiv(N, 32), 1), 256, 0, c.st>>>(a, b, 0, M, N, 0.0, c.colbuf.p, pred);
+    post_launch(c);
+    k_seqsum<<<1, 32, 0, c.st>>>(c.colbuf.p, N, nullptr, out, 1, pred);
+    post_launch(c);
+    return;
+  }
+  const int64_t total = (int64_t)M * N;
   const int g = elem_grid(total);
   k_dot_part<<<g, 256, 0, c.st>>>(total, a, b, c.part.p);
   post_launch(c);
-  reduce_to(c, c.part.p, g, out);
+  reduce_to(c, c.part.p, g, out, 1, false, 0.0, pred);
 }
 
 // Hessian-vector product of one precision: Hp = H p (BF, 246-342); masks the
@@ -394,8 +447,17 @@ static void cg_solve(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, double bdfa
   k_cg_init<T><<<g, 256, 0, c.st>>>(c.X.p, c.G.p, c.bdiag.p, bdfac, kActiveTol, M, N, c.ik.p, b.r.p, b.z.p, b.p.p,
                                     b.sn.p, c.part.p, c.part2.p, c.ipart.p);
   post_launch(c);
-  reduce_to(c, c.part.p, g, c.sc.p + SC_NORM);
-  reduce_to(c, c.part2.p, g, c.sc.p + SC_RZ);
+  constexpr bool kF64 = std::is_same<T, double>::value;
+  const bool exact = kF64 && c.exact;
+  if (exact) {
+    if constexpr (kF64) {
+      dot_dev(c, b.r.p, b.r.p, c.sc.p + SC_NORM);  // (-g).(-g) == g.g bit for bit
+      dot_dev(c, b.r.p, b.z.p, c.sc.p + SC_RZ);
+    }
+  } else {
+    reduce_to(c, c.part.p, g, c.sc.p + SC_NORM);
+    reduce_to(c, c.part2.p, g, c.sc.p + SC_RZ);
+  }
   k_sum_i<<<1, 256, 0, c.st>>>(c.ipart.p, g, c.icount.p);
   post_launch(c);
   k_cg_scalars0<<<1, 1, 0, c.st>>>(c.sc.p);
@@ -429,13 +491,22 @@ static void cg_solve(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, double bdfa
       }
       {
         Scope sb(c.timers, "BF");
-        hvp<T>(c, b, fv, tv, c.ik.p, true, c.sc.p);
+        hvp<T>(c, b, fv, tv, c.ik.p, !exact, c.sc.p);
       }
+      if constexpr (kF64)
+        if (exact) dot_dev(c, b.p.p, b.Hp.p, c.sc.p + SC_V2, c.sc.p);
       k_cg_step<T><<<g, 256, 0, c.st>>>(c.sc.p, c.bdiag.p, bdfac, M, N, b.p.p, b.Hp.p, b.sn.p, b.r.p, b.z.p, c.part.p,
                                         c.part2.p);
       post_launch(c);
-      reduce_to(c, c.part.p, g, c.sc.p + SC_RZ, 1, false, 0.0, c.sc.p);
-      reduce_to(c, c.part2.p, g, c.sc.p + SC_RR, 1, false, 0.0, c.sc.p);
+      if (exact) {
+        if constexpr (kF64) {
+          dot_dev(c, b.r.p, b.z.p, c.sc.p + SC_RZ, c.sc.p);
+          dot_dev(c, b.r.p, b.r.p, c.sc.p + SC_RR, c.sc.p);
+        }
+      } else {
+        reduce_to(c, c.part.p, g, c.sc.p + SC_RZ, 1, false, 0.0, c.sc.p);
+        reduce_to(c, c.part2.p, g, c.sc.p + SC_RR, 1, false, 0.0, c.sc.p);
+      }
       k_cg_scalars1<<<1, 1, 0, c.st>>>(c.sc.p, c.cglog.p, kMaxCG);
       post_launch(c);
     }
@@ -459,6 +530,21 @@ static void cg_solve(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, double bdfa
   }
 }
 
+// Row-wise simplex projection (doproj, 1120-1140) of X + alpha_b*S (or of X
+// when S is null) into out[b].  FP64 path: Condat's algorithm in the
+// reference's order (bitwise equal to condat_simplexproj.c), one thread per
+// row.  Mixed path: one warp per row, Michelot's fixed point.
+static void project_rows(Ctx& c, const double* X, const double* S, const double* alphas, double* out, int B) {
+  const int M = (int)c.h.M, N = (int)c.h.N;
+  const int64_t MN = (int64_t)M * N;
+  if (c.exact) {
+    k_condat<<<dim3(cdiv(M, kRowThreads), B), kRowThreads, 0, c.st>>>(X, S, alphas, out, c.aux.p, MN, M, N);
+  } else {
+    k_simplex<<<dim3(cdiv((int64_t)M * 32, 128), B), 128, 0, c.st>>>(X, S, alphas, out, MN, M, N);
+  }
+  post_launch(c);
+}
+
 // Candidates X + alpha_b*S (b < B) projected the way the stage requires and
 // rebuilt as L does, their objectives and (stage 2) xmin into c.pin.
 static void eval_candidates(Ctx& c, const double* al, int B, bool stage2, double* L, double* xmin) {
@@ -474,8 +560,7 @@ static void eval_candidates(Ctx& c, const double* al, int B, bool stage2, double
     reduce_to(c, c.part2.p, gb, c.lsout.p + 2 * kBatchLS, B, true, 0.0);
   } else {
     Scope s(c.timers, "doproj");
-    k_simplex<<<dim3(cdiv((int64_t)M * 32, 128), B), 128, 0, c.st>>>(c.X.p, c.sn64.p, c.alphas.p, c.Xc.p, MN, M, N);
-    post_launch(c);
+    project_rows(c, c.X.p, c.sn64.p, c.alphas.p, c.Xc.p, B);
   }
   {
     Scope s(c.timers, "L");
@@ -547,7 +632,12 @@ static double op_conv(Ctx& c, bool tprint) {
   k_conv_rows<<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(c.X.p, c.G.p, M, N, c.part.p,
                                                               (tprint && c.verbose) ? lam.p : nullptr);
   post_launch(c);
-  reduce_to(c, c.part.p, M, c.sc.p + SC_TMP);
+  if (c.exact) {
+    k_seqsum<<<1, 32, 0, c.st>>>(c.part.p, M, nullptr, c.sc.p + SC_TMP, 1, nullptr);
+    post_launch(c);
+  } else {
+    reduce_to(c, c.part.p, M, c.sc.p + SC_TMP);
+  }
   read_back(c, c.sc.p + SC_TMP, 1);
   const double conv = std::sqrt(c.pin[0] / ((double)N * (double)M));
   if (tprint && c.verbose) {
@@ -625,8 +715,7 @@ static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
   st.xmin = 0.0;
   if (c.fullspace) {
     Scope s(c.timers, "doproj");
-    k_simplex<<<dim3(cdiv((int64_t)M * 32, 128), 1), 128, 0, c.st>>>(c.X.p, nullptr, nullptr, c.X.p, MN, M, N);
-    post_launch(c);
+    project_rows(c, c.X.p, nullptr, nullptr, c.X.p, 1);
   } else {
     Scope s(c.timers, "doproj2");
     const int gb = cdiv(M, kRowThreads);
@@ -680,6 +769,7 @@ static void get_x_colmajor(Ctx& c, double* out) {
   std::vector<double> rm((size_t)M * N);
   CK(cudaMemcpyAsync(rm.data(), c.X.p, rm.size() * 8, cudaMemcpyDeviceToHost, c.st));
   CK(cudaStreamSynchronize(c.st));
+  c.d2h += (int64_t)rm.size() * 8;
   for (int64_t i = 0; i < M; ++i)
     for (int64_t n = 0; n < N; ++n) out[i + n * M] = rm[(size_t)i * N + n];
 }
@@ -691,6 +781,7 @@ static void set_x_colmajor(Ctx& c, const double* in) {
     for (int64_t n = 0; n < N; ++n) rm[(size_t)i * N + n] = in[i + n * M];
   CK(cudaMemcpyAsync(c.X.p, rm.data(), rm.size() * 8, cudaMemcpyHostToDevice, c.st));
   CK(cudaStreamSynchronize(c.st));
+  c.h2d += (int64_t)rm.size() * 8;
 }
 
 static void download_rowmajor_to_col(Ctx& c, const double* dev, double* out) {
@@ -723,6 +814,7 @@ static void solve(Ctx& c, int mode, int maxiiter, double conv_thres, int start_s
   c.n_cg = c.n_lsL = c.n_refine = 0;
   c.refine = false;
   CK(cudaMemcpyAsync(c.maxr.p, c.h_maxr.data(), c.h.M * 4, cudaMemcpyHostToDevice, c.st));
+  c.h2d += c.h.M * 4;
   // 1908-1915: objective and gradient of the starting point (full space).
   c.fullspace = true;
   st.L0 = op_L(c);
@@ -929,6 +1021,28 @@ int pqdts_cuda_get_x(pqdts_ctx* c, double* X) {
   });
 }
 
+int pqdts_cuda_init_x(pqdts_ctx* c) {
+  return guarded(c, [&] {
+    pqdts::need_problem(*c);
+    const int64_t MN = c->h.M * c->h.N;
+    pqdts::k_fill<<<pqdts::elem_grid(MN), 256, 0, c->st>>>(MN, 1.0 / (double)c->h.N, c->X.p);
+    pqdts::post_launch(*c);
+  });
+}
+
+int pqdts_cuda_get_stream(pqdts_ctx* c, void** stream) {
+  if (!c || !stream) return PQDTS_E_ARG;
+  *stream = (void*)c->st;
+  return PQDTS_OK;
+}
+
+int pqdts_cuda_transfer_bytes(pqdts_ctx* c, int64_t* h2d, int64_t* d2h) {
+  if (!c) return PQDTS_E_ARG;
+  if (h2d) *h2d = c->h2d.load();
+  if (d2h) *d2h = c->d2h.load();
+  return PQDTS_OK;
+}
+
 int pqdts_cuda_set_space(pqdts_ctx* c, int32_t fullspace, const int32_t* maxr) {
   return guarded(c, [&] {
     pqdts::need_problem(*c);
@@ -1017,10 +1131,7 @@ int pqdts_cuda_Bdiag(pqdts_ctx* c, double* BD) {
 int pqdts_cuda_doproj(pqdts_ctx* c) {
   return guarded(c, [&] {
     pqdts::need_problem(*c);
-    const int M = (int)c->h.M, N = (int)c->h.N;
-    pqdts::k_simplex<<<dim3(pqdts::cdiv((int64_t)M * 32, 128), 1), 128, 0, c->st>>>(c->X.p, nullptr, nullptr, c->X.p,
-                                                                                     (int64_t)M * N, M, N);
-    pqdts::post_launch(*c);
+    pqdts::project_rows(*c, c->X.p, nullptr, nullptr, c->X.p, 1);
     CK(cudaStreamSynchronize(c->st));
   });
 }
@@ -1051,11 +1162,12 @@ int pqdts_cuda_simplexproj(pqdts_ctx* c, const double* y, double* x, int64_t len
   return guarded(c, [&] {
     if (!y || !x || len <= 0 || rows <= 0) throw Err(PQDTS_E_ARG, "bad simplexproj arguments");
     if (len * rows >= ((int64_t)1 << 31)) throw Err(PQDTS_E_ARG, "simplexproj input too large");
-    pqdts::DBuf<double> d;
+    pqdts::DBuf<double> d, w;
     d.alloc((size_t)(len * rows));
+    w.alloc((size_t)(len * rows));
     CK(cudaMemcpyAsync(d.p, y, len * rows * 8, cudaMemcpyHostToDevice, c->st));
-    pqdts::k_simplex<<<dim3(pqdts::cdiv(rows * 32, 128), 1), 128, 0, c->st>>>(d.p, nullptr, nullptr, d.p, 0,
-                                                                                (int)rows, (int)len);
+    pqdts::k_condat<<<dim3(pqdts::cdiv(rows, pqdts::kRowThreads), 1), pqdts::kRowThreads, 0, c->st>>>(
+        d.p, nullptr, nullptr, d.p, w.p, 0, (int)rows, (int)len);
     pqdts::post_launch(*c);
     CK(cudaMemcpyAsync(x, d.p, len * rows * 8, cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));

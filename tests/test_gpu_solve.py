@@ -1,8 +1,17 @@
-"""Full-solve parity: the FP64 GPU solve against the oracle's solve on the same
-seeded inputs.  Tolerances are the drop-in requirement: final objective within
-1e-10 relative, Pi within 1e-8 max-abs, rows on the simplex (sums 1 within
-1e-12, entries >= 0).  The mixed-precision solve must reach an objective
-within 1e-8 relative of the FP64 solve with the same feasibility.
+"""Full-solve parity on the same seeded inputs.
+
+FP64 path: the whole trajectory (every CG iteration, line-search decision and
+stage exit) reproduces the oracle's, so the final Pi and objective are
+bit-identical -- which is stronger than the drop-in bar (objective within
+1e-10 relative, Pi within 1e-8 max-abs).  Bitwise identity is what the bar
+needs at the reference's own tolerance: at conv < 1e-6 the objective is only
+fixed to ~1e-4 relative, so two trajectories that differ by one rounding end
+~1e-4 apart.
+
+Mixed path: at a tolerance that pins the objective (conv < 1e-9), the final
+objective is within 1e-8 relative of the FP64 solve's, and Pi is feasible
+(row sums 1 within 1e-12, entries >= -1e-12 as the reference's own
+line-search bound allows).
 """
 import numpy as np
 import pytest
@@ -36,8 +45,9 @@ def test_fp64_solve_matches_oracle(built, request, which):
     X, st, launches = _solve_gpu(inst)
     Xo, so = Oracle.from_instance(inst).solve(mode=2, maxiter=200, eps=inst.eps)
     assert launches > 0
-    assert abs(st["L"] - so["L"]) <= OBJ_REL * abs(so["L"]), (st, so)
-    assert np.max(np.abs(X - Xo)) <= PI_ABS
+    assert st["L"] == so["L"] and st["outer"] == so["outer"] and st["cg"] == so["cg"], (st, so)
+    assert np.array_equal(X, Xo)
+    assert abs(st["L"] - so["L"]) <= OBJ_REL * abs(so["L"]) and np.max(np.abs(X - Xo)) <= PI_ABS
     _feasible(X)
     assert st["conv"] < inst.eps
 
@@ -47,19 +57,18 @@ def test_mode1_matches_oracle(built, small):
 
     X, st, _ = _solve_gpu(small, mode=1, maxiter=40)
     Xo, so = Oracle.from_instance(small).solve(mode=1, maxiter=40, eps=small.eps)
-    assert abs(st["L"] - so["L"]) <= OBJ_REL * abs(so["L"])
-    assert np.max(np.abs(X - Xo)) <= PI_ABS
+    assert st["L"] == so["L"] and np.array_equal(X, Xo)
     _feasible(X)
 
 
 @pytest.mark.parametrize("which", ["cfg1", "small"])
 def test_mixed_precision_solve(built, request, which):
     inst = request.getfixturevalue(which)
-    X64, s64, _ = _solve_gpu(inst, 0)
-    X32, s32, _ = _solve_gpu(inst, 1)
+    X64, s64, _ = _solve_gpu(inst, 0, maxiter=2000, eps=1e-9)
+    X32, s32, _ = _solve_gpu(inst, 1, maxiter=2000, eps=1e-9)
     assert abs(s32["L"] - s64["L"]) <= MIXED_OBJ_REL * abs(s64["L"]), (s32, s64)
     _feasible(X32)
-    assert s32["conv"] < inst.eps
+    assert s32["conv"] < 1e-9
 
 
 def test_start_stage2_and_restart(built, small):
@@ -76,8 +85,7 @@ def test_start_stage2_and_restart(built, small):
         st = s.solve(mode=2, maxiter=100, eps=small.eps, start_stage=2)
         X = s.get_x()
     Xo, so = Oracle.from_instance(small).solve(X0, mode=2, maxiter=100, eps=small.eps, start_stage=2)
-    assert abs(st["L"] - so["L"]) <= OBJ_REL * abs(so["L"])
-    assert np.max(np.abs(X - Xo)) <= PI_ABS
+    assert st["L"] == so["L"] and np.array_equal(X, Xo)
 
 
 def test_batch_matches_single(built):
@@ -88,5 +96,17 @@ def test_batch_matches_single(built):
     Xs, stats = pq.solve_batch(insts, maxiter=100)
     for inst, X, st in zip(insts, Xs, stats):
         Xs1, s1, _ = _solve_gpu(inst, maxiter=100)
-        assert abs(st["L"] - s1["L"]) <= 1e-13 * abs(s1["L"])
-        assert np.array_equal(X, Xs1)
+        assert st["L"] == s1["L"] and np.array_equal(X, Xs1)
+
+
+@pytest.mark.parametrize("which", ["cfg1", "small"])
+def test_fp64_tight_tolerance_matches_oracle(built, request, which):
+    """At conv < 1e-9 the objective is pinned; the tolerance form of the bar."""
+    from oracle.oracle import Oracle
+
+    inst = request.getfixturevalue(which)
+    X, st, _ = _solve_gpu(inst, maxiter=2000, eps=1e-9)
+    Xo, so = Oracle.from_instance(inst).solve(mode=2, maxiter=2000, eps=1e-9)
+    assert abs(st["L"] - so["L"]) <= OBJ_REL * abs(so["L"])
+    assert np.max(np.abs(X - Xo)) <= PI_ABS
+    _feasible(X)
