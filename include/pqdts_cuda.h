@@ -131,6 +131,11 @@ typedef void (*pqdts_stage_cb)(void* user, int32_t oiter, const double* X_colmaj
 int pqdts_cuda_solve(pqdts_ctx* ctx, int32_t mode, int32_t maxiiter, double conv_thres, int32_t start_stage,
                      int32_t output, pqdts_stage_cb stage_cb, void* user, double* stats);
 
+/* Optional extra stopping rule (not in the reference, off by default): end
+ * the solve as soon as an outer iteration's objective L <= target (target
+ * <= 0 disables it).  Used to time a solver to a given objective. */
+int pqdts_cuda_set_objective_target(pqdts_ctx* ctx, double target);
+
 /* Accumulated GPU time (CUDA events) of a named region of the reference's
  * timers ("L", "dL", "BF", "CG", "Lalpha_min", "doproj", "doproj2", "min"). */
 int pqdts_cuda_timer(pqdts_ctx* ctx, const char* name, double* seconds, int64_t* count);

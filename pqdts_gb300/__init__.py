@@ -72,6 +72,7 @@ def lib():
         "pqdts_cuda_run_stage": [p, i32, i32, i32, d, i32, p],
         "pqdts_cuda_solve": [p, i32, i32, d, i32, i32, p, p, p],
         "pqdts_cuda_timer": [p, C.c_char_p, C.POINTER(d), C.POINTER(i64)],
+        "pqdts_cuda_set_objective_target": [p, d],
         "pqdts_cuda_solve_batch": [i32, i32, p, p, p, p, p, p, p, p, p, p, p, i32, i32, i32, d, p, p],
     }
     for name, args in sig.items():
@@ -257,6 +258,10 @@ class Solver:
         self._check(self._L.pqdts_cuda_run_stage(self.h, int(mode), int(oiter), int(maxiter), float(eps),
                                                  int(output), _ptr(stats)), "run_stage")
         return dict(zip(STAT_KEYS, stats.tolist()))
+
+    def set_objective_target(self, target):
+        """Extra stopping rule (off by default): stop once L <= target."""
+        self._check(self._L.pqdts_cuda_set_objective_target(self.h, float(target)), "set_objective_target")
 
     def kernel_launches(self):
         v = C.c_int64()

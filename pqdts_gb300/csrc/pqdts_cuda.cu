@@ -205,6 +205,8 @@ struct pqdts_ctx {
   pqdts::GpuTimers timers;
   int64_t n_cg = 0, n_lsL = 0, n_refine = 0;
   bool refine = false;  // mixed precision: FP64 CG from now on
+  double target_L = 0.0;  // optional objective stopping rule (0 = off)
+  bool target_hit = false;
 };
 
 namespace pqdts {
@@ -759,6 +761,10 @@ static void run_stage(Ctx& c, int mode, int oiter, int maxiiter, double conv_thr
     outer_iteration(c, mode, oiter, st);
     print_iter(c, oiter, iiter, mode, st, t1);
     if (st.conv < conv_thres) break;
+    if (c.target_L > 0 && st.L0 <= c.target_L) {
+      c.target_hit = true;
+      break;
+    }
   }
   st.conv = op_conv(c, output >= 3);
   c.timers.flush();
@@ -830,7 +836,8 @@ static void solve(Ctx& c, int mode, int maxiiter, double conv_thres, int start_s
   const double t0 = wall();
   st.t0 = t0;
   const int tmin = c.timers.begin("min");
-  for (int oiter = start_stage; oiter <= 2; ++oiter) {
+  c.target_hit = false;
+  for (int oiter = start_stage; oiter <= 2 && !c.target_hit; ++oiter) {
     run_stage(c, mode, oiter, maxiiter, conv_thres, output, st);
     if (cb) {
       std::vector<double> xh((size_t)c.h.M * c.h.N);
@@ -1193,6 +1200,12 @@ int pqdts_cuda_run_stage(pqdts_ctx* c, int32_t mode, int32_t oiter, int32_t maxi
 int pqdts_cuda_solve(pqdts_ctx* c, int32_t mode, int32_t maxiiter, double conv_thres, int32_t start_stage,
                      int32_t output, pqdts_stage_cb cb, void* user, double* stats) {
   return guarded(c, [&] { pqdts::solve(*c, mode, maxiiter, conv_thres, start_stage, output, cb, user, stats); });
+}
+
+int pqdts_cuda_set_objective_target(pqdts_ctx* c, double target) {
+  if (!c) return PQDTS_E_ARG;
+  c->target_L = target > 0 ? target : 0.0;
+  return PQDTS_OK;
 }
 
 int pqdts_cuda_timer(pqdts_ctx* c, const char* name, double* seconds, int64_t* count) {

@@ -26,7 +26,7 @@ import math
 import os
 
 import numpy as np
-from scipy import special, stats
+from scipy import stats
 
 CUTOFF = 1e-16
 
@@ -82,21 +82,73 @@ class Instance:
         return F
 
 
+# Elementary functions from IEEE basic operations only (+, -, *, /, rint,
+# ldexp, frexp), so the generated F is bit-identical on every platform
+# (numpy's vectorised exp/log differ between x86 and aarch64 builds).
+_LN2_HI = 6.93147180369123816490e-01
+_LN2_LO = 1.90821492927058770002e-10
+_INV_LN2 = 1.44269504088896338700e+00
+
+
+def det_exp(t):
+    t = np.asarray(t, dtype=np.float64)
+    k = np.rint(t * _INV_LN2)
+    r = (t - k * _LN2_HI) - k * _LN2_LO
+    # Taylor series of e^r, |r| <= 0.35: 18 terms reach 1e-17
+    p = np.ones_like(r)
+    term = np.ones_like(r)
+    for n in range(1, 19):
+        term = term * r / n
+        p = p + term
+    return np.ldexp(p, k.astype(np.int64))
+
+
+def det_log(x):
+    x = np.asarray(x, dtype=np.float64)
+    m, e = np.frexp(x)  # x = m * 2^e, m in [0.5, 1)
+    small = m < 0.7071067811865476
+    m = np.where(small, m * 2.0, m)
+    e = np.where(small, e - 1, e).astype(np.float64)
+    s = (m - 1.0) / (m + 1.0)  # |s| < 0.172
+    s2 = s * s
+    acc = np.zeros_like(s)
+    for n in range(27, 0, -2):
+        acc = acc * s2 + 1.0 / n
+    return (e * _LN2_HI + 2.0 * s * acc) + e * _LN2_LO
+
+
+def det_log_factorial(i):
+    """log(i!) for integer arrays i >= 0 (Stirling series above 16)."""
+    i = np.asarray(i, dtype=np.int64)
+    out = np.zeros(i.shape, dtype=np.float64)
+    fact = np.cumprod(np.concatenate([[1.0], np.arange(1, 17, dtype=np.float64)]))  # exact up to 16!
+    lo = i <= 16
+    out[lo] = det_log(fact[i[lo]])
+    z = (i[~lo] + 1).astype(np.float64)
+    zi = 1.0 / z
+    zi2 = zi * zi
+    series = zi * (1.0 / 12 - zi2 * (1.0 / 360 - zi2 * (1.0 / 1260 - zi2 * (1.0 / 1680 - zi2 / 1188))))
+    half_log_2pi = 0.91893853320467274178
+    out[~lo] = (z - 0.5) * det_log(z) - z + half_log_2pi + series
+    return out
+
+
 def poisson_bands(M: int, D: int, xmax: float, cutoff: float = CUTOFF):
     """Row windows of F[d, i] = Poisson pmf(i; x_d), x_d = linspace(0.01, xmax, D)."""
     x = np.linspace(0.01, xmax, D)
     lo = np.full(D, -1, dtype=np.int64)
     hi = np.full(D, -1, dtype=np.int64)
     vals = []
+    logx = det_log(x)
     for d in range(D):
-        xd = x[d]
+        xd = float(x[d])
         half = 12.0 * math.sqrt(xd) + 40.0
         a = max(0, int(math.floor(xd - half)))
         b = min(M - 1, int(math.ceil(xd + half)))
         if a > b:
             continue
-        i = np.arange(a, b + 1, dtype=np.float64)
-        p = np.exp(i * math.log(xd) - xd - special.gammaln(i + 1.0))
+        ii = np.arange(a, b + 1, dtype=np.int64)
+        p = det_exp(ii * logx[d] - xd - det_log_factorial(ii))
         keep = np.nonzero(p >= cutoff)[0]
         if keep.size == 0:
             continue
