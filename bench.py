@@ -431,18 +431,45 @@ def run_ours(args):
     return 0
 
 
-def run_profile_case(precision):
-    """A short solve of the benchmark workload (one outer iteration per
-    stage) whose launches ncu can list and capture in a minute or two."""
+def run_profile_case(case):
+    """Launches for ncu on the benchmark workload.
+      fp64 / mixed: the Hessian product (3x BF resp. BF32), then 3x dL and
+        3x L at a random feasible X -- real banded-product launches only;
+      solve64 / solvemix: one full benchmark solve (the launch list)."""
+    import numpy as np
+
     import pqdts_gb300 as pq
     from pqdts_gb300 import synth
 
     inst = synth.make_config(CONFIG, seed=0)
+    prec = pq.MIXED if case in ("mixed", "solvemix") else pq.FP64
     with pq.Solver(0) as s:
-        s.set_instance(inst, pq.MIXED if precision == "mixed" else pq.FP64)
-        s.init_x()
-        st = s.solve(mode=2, maxiter=1, eps=EPS)
-        print(json.dumps({"profile_case": precision, "stats": st, "launches": s.kernel_launches()}))
+        s.set_instance(inst, prec)
+        if case.startswith("solve"):
+            L64 = None
+            if prec == pq.MIXED:
+                with pq.Solver(0) as s64:
+                    s64.set_instance(inst, pq.FP64)
+                    L64 = s64.solve(mode=2, maxiter=MAXITER, eps=EPS)["L"]
+                s.set_objective_target(L64 * (1 + OBJ_REL))
+            s.init_x()
+            st = s.solve(mode=2, maxiter=MAXITER, eps=EPS if prec == pq.FP64 else 1e-300)
+            print(json.dumps({"profile_case": case, "stats": st, "launches": s.kernel_launches()}))
+            return 0
+        rng = np.random.default_rng(0)
+        X = rng.random((inst.M, inst.N))
+        X /= X.sum(1, keepdims=True)
+        s.set_x(X)
+        V = rng.standard_normal((inst.M, inst.N))
+        for _ in range(3):
+            (s.BF32 if prec == pq.MIXED else s.BF)(V)
+        for _ in range(3):
+            s.set_x(X)
+            s.dL()
+        for _ in range(3):
+            s.set_x(X)
+            s.L()
+        print(json.dumps({"profile_case": case, "launches": s.kernel_launches()}))
     return 0
 
 
@@ -458,8 +485,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-iters", type=int, default=4)
     ap.add_argument("--ref-sample-iters", type=int, default=3)
-    ap.add_argument("--profile-case", choices=["fp64", "mixed"], default=None,
-                    help="one short solve (1 iteration per stage) of the workload, for ncu")
+    ap.add_argument("--profile-case", choices=["fp64", "mixed", "solve64", "solvemix"], default=None,
+                    help="launches of the workload for ncu (see run_profile_case)")
     args = ap.parse_args()
     if args.profile_case:
         return run_profile_case(args.profile_case)

@@ -99,6 +99,9 @@ int pqdts_cuda_dL(pqdts_ctx* ctx, double* G_colmajor);             /* dL, pqdts.
 int pqdts_cuda_redO(pqdts_ctx* ctx, double* O_ND);                 /* redO local part, 707-736 */
 int pqdts_cuda_BF(pqdts_ctx* ctx, const double* V_colmajor, double* HV_colmajor); /* BF, 246-342 (FP64) */
 int pqdts_cuda_Bdiag(pqdts_ctx* ctx, double* BD_colmajor);         /* Bdiag, 208-244 */
+/* BF in the mixed-precision solver's arithmetic (FP32 values and
+ * accumulation; PQDTS_MIXED problems only): the CG's Hessian product. */
+int pqdts_cuda_BF32(pqdts_ctx* ctx, const double* V_colmajor, double* HV_colmajor);
 int pqdts_cuda_doproj(pqdts_ctx* ctx);                              /* doproj, 1120-1140 */
 int pqdts_cuda_doproj2(pqdts_ctx* ctx, double* xmin);              /* doproj2, 1142-1164 */
 int pqdts_cuda_conv_test(pqdts_ctx* ctx, double* conv);            /* conv_test, 1034-1067 */

@@ -64,6 +64,7 @@ def lib():
         "pqdts_cuda_dL": [p, p],
         "pqdts_cuda_redO": [p, p],
         "pqdts_cuda_BF": [p, p, p],
+        "pqdts_cuda_BF32": [p, p, p],
         "pqdts_cuda_Bdiag": [p, p],
         "pqdts_cuda_doproj": [p],
         "pqdts_cuda_doproj2": [p, C.POINTER(d)],
@@ -219,6 +220,13 @@ class Solver:
         V = np.asfortranarray(V, np.float64)
         H = np.empty((self.M, self.N), order="F")
         self._check(self._L.pqdts_cuda_BF(self.h, _ptr(V), _ptr(H)), "BF")
+        return H
+
+    def BF32(self, V):
+        """The mixed-precision solver's FP32 Hessian product (mixed problems)."""
+        V = np.asfortranarray(V, np.float64)
+        H = np.empty((self.M, self.N), order="F")
+        self._check(self._L.pqdts_cuda_BF32(self.h, _ptr(V), _ptr(H)), "BF32")
         return H
 
     def Bdiag(self):

@@ -119,9 +119,21 @@ struct GpuTimers {
     counts[p.id]++;
     return (int)pending.size() - 1;
   }
-  void end(int tok) {
-    pending[tok].b = ev();
-    CK(cudaEventRecord(pending[tok].b, st));
+  // Called from destructors: never throws; a failed record only loses the
+  // sample (the CUDA error itself surfaces at the next checked call).
+  void end(int tok) noexcept {
+    cudaEvent_t e = nullptr;
+    if (!pool.empty()) {
+      e = pool.back();
+      pool.pop_back();
+    } else if (cudaEventCreate(&e) != cudaSuccess) {
+      return;
+    }
+    if (cudaEventRecord(e, st) != cudaSuccess) {
+      pool.push_back(e);
+      return;
+    }
+    pending[tok].b = e;
   }
   void flush() {
     if (pending.empty()) return;
@@ -206,6 +218,10 @@ struct pqdts_ctx {
   int64_t n_cg = 0, n_lsL = 0, n_refine = 0;
   bool refine = false;  // mixed precision: FP64 CG from now on
   double target_L = 0.0;  // optional objective stopping rule (0 = off)
+  // version of X, bumped on every write; results keyed on it are reused
+  int64_t xver = 0, R_ver = -1, G_ver = -1, L_ver = -1;
+  bool G_full = true;
+  double L_cache = 0.0;
   bool target_hit = false;
 };
 
@@ -227,6 +243,9 @@ static DevBands bands_of(Ctx& c) {
 }
 
 static inline int cdiv(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+// X changed: results keyed on the old version are stale.
+static void touch_x(Ctx& c) { c.xver++; }
 
 static void post_launch(Ctx& c) {
   c.launches++;
@@ -274,13 +293,11 @@ static void setup_device(Ctx& c) {
   }
   c.cg64.alloc(MN, M, D * N);
   c.exact = (c.precision == PQDTS_FP64);
-  if (c.exact) {
-    c.Rst.alloc((size_t)kBatchLS * D * N);
-    c.aux.alloc((size_t)kBatchLS * MN);
-  } else {
-    c.Rst.release();
-    c.aux.release();
-  }
+  // residual stack of the line-search candidates (both precisions)
+  c.Rst.alloc((size_t)kBatchLS * D * N);
+  // Condat scratch rows (FP64 path only; the mixed path projects in place)
+  if (c.exact) c.aux.alloc((size_t)kBatchLS * MN);
+  else c.aux.release();
   c.srow.alloc((size_t)kBatchLS * std::max(D, M));
   c.gcol.alloc((size_t)kBatchLS * N);
   c.colbuf.alloc(N);
@@ -305,6 +322,8 @@ static void setup_device(Ctx& c) {
   // Initial X = 1/N (pqdts.f90:1834-1838) and maxr from the seeded stream.
   k_fill<<<elem_grid(MN), 256, 0, c.st>>>(MN, 1.0 / (double)N, c.X.p);
   post_launch(c);
+  c.R_ver = c.G_ver = c.L_ver = -1;
+  touch_x(c);
   CK(cudaMemcpyAsync(c.maxr.p, c.h_maxr.data(), M * 4, cudaMemcpyHostToDevice, c.st));
   c.h2d += M * 4;
   CK(cudaStreamSynchronize(c.st));
@@ -325,23 +344,14 @@ static void rebuild(Ctx& c, double* X, int B = 1) {
   post_launch(c);
 }
 
-// Objective of B stacked, already projected/rebuilt matrices; the values
-// land in c.pin after fetch_objectives.  FP64 path: O - P is stored and
-// summed in the oracle's order (row chains over n, rows in ascending order,
-// then the gamma term's column chains added column by column).  Mixed path:
-// fixed-shape tree reductions.
-static void objective_stack(Ctx& c, const double* Xs, int B) {
+// Objective from the per-row residual sums srow[b][d] of B matrices Xs
+// (L_red) plus the gamma term of Xs (L_gam, 954-964) -> lsout[b].  FP64 path:
+// rows added in ascending order, then the gamma term's column chains added
+// column by column (the oracle's order).  Mixed path: fixed-shape trees.
+static void objective_combine(Ctx& c, const double* Xs, int B) {
   const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
-  DevBands bd = bands_of(c);
-  dim3 grid(cdiv(N, kBX), cdiv(D, kBY), B);
   if (c.exact) {
-    k_fwd<double, 3><<<grid, dim3(kBX, kBY), 0, c.st>>>(bd, c.fval.p, Xs, (int64_t)M * N, c.P.p, c.Rst.p, nullptr,
-                                                        nullptr);
-    post_launch(c);
-    k_rowchain_resid<<<dim3(cdiv(D, kRowThreads), B), kRowThreads, 0, c.st>>>(c.Rst.p, c.flo.p, D, N, c.srow.p);
-    post_launch(c);
-    double* out = c.lsout.p;
-    if (c.h.gam != 0) out = c.lred.p;
+    double* out = c.h.gam != 0 ? c.lred.p : c.lsout.p;
     k_seqsum<<<1, 32, 0, c.st>>>(c.srow.p, D, nullptr, out, B, nullptr);
     post_launch(c);
     if (c.h.gam != 0) {
@@ -354,10 +364,7 @@ static void objective_stack(Ctx& c, const double* Xs, int B) {
     CK(cudaMemsetAsync(c.lsout.p + kBatchLS, 0, B * sizeof(double), c.st));
     return;
   }
-  k_fwd<double, 2><<<grid, dim3(kBX, kBY), 0, c.st>>>(bd, c.fval.p, Xs, (int64_t)M * N, c.P.p, nullptr, c.part.p,
-                                                      nullptr);
-  post_launch(c);
-  reduce_to(c, c.part.p, (int64_t)grid.x * grid.y, c.lsout.p, B);
+  reduce_to(c, c.srow.p, D, c.lsout.p, B);
   if (c.h.gam != 0) {
     const int g = elem_grid((int64_t)(M - 1) * N);
     k_gamma_part<<<dim3(g, B), 256, 0, c.st>>>(Xs, (int64_t)M * N, M, N, c.h.gam, c.part2.p);
@@ -368,35 +375,122 @@ static void objective_stack(Ctx& c, const double* Xs, int B) {
   }
 }
 
+// Objective of B stacked, already projected/rebuilt candidates: O - P of
+// each into the residual stack, per-row chains, then objective_combine.
+static void require(const void* p, const char* what) {
+  if (p == nullptr) throw Err(PQDTS_E_STATE, std::string("internal: device buffer ") + what + " is not allocated");
+}
+
+static void objective_stack(Ctx& c, const double* Xs, int B) {
+  const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
+  require(c.Rst.p, "Rst");
+  if (B < 1 || B > kBatchLS) throw Err(PQDTS_E_STATE, "internal: candidate batch out of range");
+  DevBands bd = bands_of(c);
+  dim3 grid(cdiv(N, kBX), cdiv(D, kBY), B);
+  k_fwd<double, 3><<<grid, dim3(kBX, kBY), 0, c.st>>>(bd, c.fval.p, Xs, (int64_t)M * N, c.P.p, c.Rst.p, nullptr,
+                                                      nullptr);
+  post_launch(c);
+  k_rowchain_resid<<<dim3(cdiv(D, kRowThreads), B), kRowThreads, 0, c.st>>>(c.Rst.p, c.flo.p, D, N, 1.0, c.srow.p);
+  post_launch(c);
+  objective_combine(c, Xs, B);
+}
+
 static void fetch_objectives(Ctx& c, int B, double* L) {
   CK(cudaMemcpyAsync(c.pin, c.lsout.p, 4 * kBatchLS * sizeof(double), cudaMemcpyDeviceToHost, c.st));
   CK(cudaStreamSynchronize(c.st));
   for (int b = 0; b < B; ++b) L[b] = (c.h.gam != 0 && !c.exact) ? c.pin[b] + c.pin[kBatchLS + b] : c.pin[b];
 }
 
-// L(X) on the context's X (917-973).
+static void rebuild_x(Ctx& c) {
+  rebuild(c, c.X.p);
+  touch_x(c);
+}
+
+// R = 2*(O - P) with O = F.X for the context's X, unless R already holds it
+// for this version of X.
+static void ensure_R(Ctx& c) {
+  if (c.R_ver == c.xver) return;
+  const int N = (int)c.h.N, D = (int)c.h.D;
+  DevBands bd = bands_of(c);
+  k_fwd<double, 0><<<dim3(cdiv(N, kBX), cdiv(D, kBY), 1), dim3(kBX, kBY), 0, c.st>>>(bd, c.fval.p, c.X.p, 0, c.P.p,
+                                                                                     c.R.p, nullptr, nullptr);
+  post_launch(c);
+  c.R_ver = c.xver;
+}
+
+// L(X) on the context's X (917-973).  The residual sums come from R (exactly
+// O - P = R/2), so L and dL of one X share one banded product.
 static double op_L(Ctx& c) {
   Scope s(c.timers, "L");
-  if (!c.fullspace) rebuild(c, c.X.p);
-  objective_stack(c, c.X.p, 1);
+  if (!c.fullspace) rebuild_x(c);
+  if (c.L_ver == c.xver) return c.L_cache;
+  ensure_R(c);
+  const int D = (int)c.h.D, N = (int)c.h.N;
+  k_rowchain_resid<<<dim3(cdiv(D, kRowThreads), 1), kRowThreads, 0, c.st>>>(c.R.p, c.flo.p, D, N, 0.5, c.srow.p);
+  post_launch(c);
+  objective_combine(c, c.X.p, 1);
   double L;
   fetch_objectives(c, 1, &L);
+  c.L_cache = L;
+  c.L_ver = c.xver;
   return L;
 }
 
-// dL(X) -> G (975-1032).
-static void op_dL(Ctx& c, double* X, double* G) {
-  Scope s(c.timers, "dL");
-  const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
-  if (!c.fullspace) rebuild(c, X);
+// Block shape of k_trans: threads x C columns per pass with the fewest idle
+// lanes (an idle lane still costs its FP64 issue slot).
+struct TransShape {
+  int threads, C;
+};
+static TransShape trans_shape(int N) {
+  TransShape best{32, 1};
+  int64_t best_waste = INT64_MAX;
+  for (int C : {1, 2, 4, 8})
+    for (int t = 32; t <= 256; t += 32) {
+      const int64_t per = (int64_t)t * C;
+      const int64_t passes = (N + per - 1) / per;
+      const int64_t waste = passes * per - N;
+      if (waste < best_waste) {
+        best_waste = waste;
+        best = {t, C};
+      }
+    }
+  return best;
+}
+
+template <typename T, bool HVP>
+static void launch_trans(Ctx& c, const T* tv, const T* R, const T* V, const T* rs, int reduced, T c2gam,
+                         const int8_t* ik, T* G, const T* W, double* dpart, const double* pred) {
+  const int M = (int)c.h.M;
+  const TransShape sh = trans_shape((int)c.h.N);
   DevBands bd = bands_of(c);
-  k_fwd<double, 0><<<dim3(cdiv(N, kBX), cdiv(D, kBY), 1), dim3(kBX, kBY), 0, c.st>>>(bd, c.fval.p, X, 0, c.P.p,
-                                                                                     c.R.p, nullptr, nullptr);
+  switch (sh.C) {
+    case 1:
+      k_trans<T, HVP, 1><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred);
+      break;
+    case 2:
+      k_trans<T, HVP, 2><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred);
+      break;
+    case 4:
+      k_trans<T, HVP, 4><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred);
+      break;
+    default:
+      k_trans<T, HVP, 8><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred);
+      break;
+  }
   post_launch(c);
-  const int tb = std::min(256, std::max(32, cdiv(cdiv(N, 4), 32) * 32));
-  k_trans<double, false><<<M, tb, 0, c.st>>>(bd, c.tval.p, c.R.p, X, nullptr, c.maxr.p, c.fullspace ? 0 : 1,
-                                             2.0 * c.h.gam, nullptr, G, nullptr, nullptr, nullptr);
-  post_launch(c);
+}
+
+// dL(X) -> c.G (975-1032), reusing R and the gradient itself when X and the
+// space have not changed since they were computed (bitwise the same values).
+static void op_dL(Ctx& c) {
+  Scope s(c.timers, "dL");
+  if (!c.fullspace) rebuild_x(c);
+  if (c.G_ver == c.xver && c.G_full == c.fullspace) return;
+  ensure_R(c);
+  launch_trans<double, false>(c, c.tval.p, c.R.p, c.X.p, nullptr, c.fullspace ? 0 : 1, 2.0 * c.h.gam, nullptr, c.G.p,
+                              nullptr, nullptr, nullptr);
+  c.G_ver = c.xver;
+  c.G_full = c.fullspace;
 }
 
 // pdot (589-614): sum(a.b) over M*N -> device scalar `out`.  FP64 path: one
@@ -429,11 +523,9 @@ static void hvp(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, const int8_t* ik
   k_fwd<T, 1><<<dim3(cdiv(N, kBX), cdiv(D, kBY), 1), dim3(kBX, kBY), 0, c.st>>>(bd, fv, src, 0, nullptr, b.R2.p,
                                                                                 nullptr, pred);
   post_launch(c);
-  const int tb = std::min(256, std::max(32, cdiv(cdiv(N, 4), 32) * 32));
-  k_trans<T, true><<<M, tb, 0, c.st>>>(bd, tv, b.R2.p, b.p.p, c.fullspace ? nullptr : b.rs.p, c.maxr.p,
-                                       c.fullspace ? 0 : 1, (T)(2.0 * c.h.gam), ik, b.Hp.p,
-                                       with_dot ? b.p.p : nullptr, with_dot ? c.part.p : nullptr, pred);
-  post_launch(c);
+  launch_trans<T, true>(c, tv, b.R2.p, b.p.p, c.fullspace ? nullptr : b.rs.p, c.fullspace ? 0 : 1,
+                        (T)(2.0 * c.h.gam), ik, b.Hp.p, with_dot ? b.p.p : nullptr, with_dot ? c.part.p : nullptr,
+                        pred);
   if (with_dot) reduce_to(c, c.part.p, M, c.sc.p + SC_V2, 1, false, 0.0, pred);
 }
 
@@ -442,6 +534,9 @@ static void hvp(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, const int8_t* ik
 // ---------------------------------------------------------------------------
 template <typename T>
 static void cg_solve(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, double bdfac, int64_t* nact_out) {
+  require(fv, "F values");
+  require(tv, "F^T values");
+  require(b.r.p, "CG vectors");
   const int M = (int)c.h.M, N = (int)c.h.N;
   const int64_t MN = (int64_t)M * N;
   const int g = elem_grid(MN);
@@ -540,6 +635,7 @@ static void project_rows(Ctx& c, const double* X, const double* S, const double*
   const int M = (int)c.h.M, N = (int)c.h.N;
   const int64_t MN = (int64_t)M * N;
   if (c.exact) {
+    require(c.aux.p, "aux");
     k_condat<<<dim3(cdiv(M, kRowThreads), B), kRowThreads, 0, c.st>>>(X, S, alphas, out, c.aux.p, MN, M, N);
   } else {
     k_simplex<<<dim3(cdiv((int64_t)M * 32, 128), B), 128, 0, c.st>>>(X, S, alphas, out, MN, M, N);
@@ -626,9 +722,9 @@ static void line_search(Ctx& c, bool stage2, double& alpha, double& dlalpha) {
 static double op_conv(Ctx& c, bool tprint) {
   Scope s(c.timers, "conv_test");
   const int M = (int)c.h.M, N = (int)c.h.N;
-  if (!c.fullspace) rebuild(c, c.X.p);
+  if (!c.fullspace) rebuild_x(c);
   c.fullspace = true;
-  op_dL(c, c.X.p, c.G.p);
+  op_dL(c);
   DBuf<double> lam;
   if (tprint && c.verbose) lam.alloc(M);
   k_conv_rows<<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(c.X.p, c.G.p, M, N, c.part.p,
@@ -681,7 +777,8 @@ static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
     c.fullspace = false;
     k_stage2_start<<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(c.X.p, c.maxr.p, M, N, 0);
     post_launch(c);
-    op_dL(c, c.X.p, c.G.p);
+    touch_x(c);
+    op_dL(c);
     k_neg_copy<<<g, 256, 0, c.st>>>(MN, c.G.p, c.sn64.p);
     post_launch(c);
     line_search(c, true, st.alpha, st.dlalpha);
@@ -690,16 +787,17 @@ static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
     if (!c.fullspace) {
       k_stage2_start<<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(c.X.p, c.maxr.p, M, N, 1);
       post_launch(c);
+      touch_x(c);
     } else {
       set_full_space(c);
     }
-    op_dL(c, c.X.p, c.G.p);
+    op_dL(c);
     const double bdfac = c.fullspace ? 1.0 : 2.0;
     const bool fp32 = (c.precision == PQDTS_MIXED) && !c.refine;
     if (fp32) cg_solve<float>(c, c.cg32, c.fval32.p, c.tval32.p, bdfac, nullptr);
     else cg_solve<double>(c, c.cg64, c.fval.p, c.tval.p, bdfac, nullptr);
     if (c.precision == PQDTS_MIXED && c.refine) c.n_refine++;
-    op_dL(c, c.X.p, c.G.p);
+    op_dL(c);
     const int32_t* mr = c.fullspace ? nullptr : c.maxr.p;
     if (fp32) k_twometric<float><<<g, 256, 0, c.st>>>(c.cg32.sn.p, c.G.p, c.ik.p, mr, c.bdiag.p, bdfac, M, N, c.sn64.p);
     else k_twometric<double><<<g, 256, 0, c.st>>>(c.cg64.sn.p, c.G.p, c.ik.p, mr, c.bdiag.p, bdfac, M, N, c.sn64.p);
@@ -713,23 +811,26 @@ static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
   if (st.alpha != 0.0) {
     k_axpy<<<g, 256, 0, c.st>>>(MN, st.alpha, c.sn64.p, c.X.p);
     post_launch(c);
+    touch_x(c);
   }
   st.xmin = 0.0;
   if (c.fullspace) {
     Scope s(c.timers, "doproj");
     project_rows(c, c.X.p, nullptr, nullptr, c.X.p, 1);
+    touch_x(c);
   } else {
     Scope s(c.timers, "doproj2");
     const int gb = cdiv(M, kRowThreads);
     k_cand_proj2<<<dim3(gb, 1), kRowThreads, 0, c.st>>>(c.X.p, nullptr, nullptr, c.X.p, MN, c.maxr.p, M, N, 0,
                                                          c.part2.p);
     post_launch(c);
+    touch_x(c);
     reduce_to(c, c.part2.p, gb, c.sc.p + SC_TMP, 1, true, 0.0);
     read_back(c, c.sc.p + SC_TMP, 1);
     st.xmin = c.pin[0];
   }
   st.L0 = op_L(c);
-  op_dL(c, c.X.p, c.G.p);
+  op_dL(c);
   dot_dev(c, c.G.p, c.G.p, c.sc.p + SC_TMP);
   read_back(c, c.sc.p + SC_TMP, 1);
   st.norm_der = c.pin[0];
@@ -788,6 +889,7 @@ static void set_x_colmajor(Ctx& c, const double* in) {
   CK(cudaMemcpyAsync(c.X.p, rm.data(), rm.size() * 8, cudaMemcpyHostToDevice, c.st));
   CK(cudaStreamSynchronize(c.st));
   c.h2d += (int64_t)rm.size() * 8;
+  touch_x(c);
 }
 
 static void download_rowmajor_to_col(Ctx& c, const double* dev, double* out) {
@@ -821,10 +923,11 @@ static void solve(Ctx& c, int mode, int maxiiter, double conv_thres, int start_s
   c.refine = false;
   CK(cudaMemcpyAsync(c.maxr.p, c.h_maxr.data(), c.h.M * 4, cudaMemcpyHostToDevice, c.st));
   c.h2d += c.h.M * 4;
+  touch_x(c);
   // 1908-1915: objective and gradient of the starting point (full space).
   c.fullspace = true;
   st.L0 = op_L(c);
-  op_dL(c, c.X.p, c.G.p);
+  op_dL(c);
   dot_dev(c, c.G.p, c.G.p, c.sc.p + SC_TMP);
   read_back(c, c.sc.p + SC_TMP, 1);
   st.norm_der = c.pin[0];
@@ -1034,6 +1137,7 @@ int pqdts_cuda_init_x(pqdts_ctx* c) {
     const int64_t MN = c->h.M * c->h.N;
     pqdts::k_fill<<<pqdts::elem_grid(MN), 256, 0, c->st>>>(MN, 1.0 / (double)c->h.N, c->X.p);
     pqdts::post_launch(*c);
+    pqdts::touch_x(*c);
   });
 }
 
@@ -1063,6 +1167,7 @@ int pqdts_cuda_set_space(pqdts_ctx* c, int32_t fullspace, const int32_t* maxr) {
       CK(cudaMemcpyAsync(c->maxr.p, maxr, c->h.M * 4, cudaMemcpyHostToDevice, c->st));
       c->fullspace = false;
     }
+    pqdts::touch_x(*c);  // maxr and the space key the cached gradient
     CK(cudaStreamSynchronize(c->st));
   });
 }
@@ -1085,7 +1190,7 @@ int pqdts_cuda_L(pqdts_ctx* c, double* val) {
 int pqdts_cuda_dL(pqdts_ctx* c, double* G) {
   return guarded(c, [&] {
     pqdts::need_problem(*c);
-    pqdts::op_dL(*c, c->X.p, c->G.p);
+    pqdts::op_dL(*c);
     pqdts::download_rowmajor_to_col(*c, c->G.p, G);
   });
 }
@@ -1100,6 +1205,7 @@ int pqdts_cuda_redO(pqdts_ctx* c, double* O) {
                               dim3(pqdts::kBX, pqdts::kBY), 0, c->st>>>(bd, c->fval.p, c->X.p, 0, nullptr, c->R.p,
                                                                         nullptr, nullptr);
     pqdts::post_launch(*c);
+    c->R_ver = -1;  // R now holds 2*O, not 2*(O - P)
     CK(cudaMemcpyAsync(O, c->R.p, (size_t)D * N * 8, cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     for (size_t k = 0; k < (size_t)D * N; ++k) O[k] *= 0.5;
@@ -1125,6 +1231,31 @@ int pqdts_cuda_BF(pqdts_ctx* c, const double* V, double* HV) {
   });
 }
 
+int pqdts_cuda_BF32(pqdts_ctx* c, const double* V, double* HV) {
+  return guarded(c, [&] {
+    pqdts::need_problem(*c);
+    if (c->precision != PQDTS_MIXED) throw Err(PQDTS_E_STATE, "BF32 needs a mixed-precision problem");
+    const int64_t M = c->h.M, N = c->h.N;
+    std::vector<float> rm((size_t)M * N);
+    for (int64_t i = 0; i < M; ++i)
+      for (int64_t n = 0; n < N; ++n) rm[(size_t)i * N + n] = (float)V[i + n * M];
+    auto& b = c->cg32;
+    CK(cudaMemcpyAsync(b.p.p, rm.data(), rm.size() * 4, cudaMemcpyHostToDevice, c->st));
+    c->h2d += (int64_t)rm.size() * 4;
+    if (!c->fullspace) {
+      pqdts::k_cg_lift<float><<<pqdts::cdiv(M, pqdts::kRowThreads), pqdts::kRowThreads, 0, c->st>>>(
+          nullptr, 0, (int)M, (int)N, b.p.p, b.z.p, c->maxr.p, b.V.p, b.rs.p);
+      pqdts::post_launch(*c);
+    }
+    pqdts::hvp<float>(*c, b, c->fval32.p, c->tval32.p, nullptr, false);
+    CK(cudaMemcpyAsync(rm.data(), b.Hp.p, rm.size() * 4, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    c->d2h += (int64_t)rm.size() * 4;
+    for (int64_t i = 0; i < M; ++i)
+      for (int64_t n = 0; n < N; ++n) HV[i + n * M] = rm[(size_t)i * N + n];
+  });
+}
+
 int pqdts_cuda_Bdiag(pqdts_ctx* c, double* BD) {
   return guarded(c, [&] {
     pqdts::need_problem(*c);
@@ -1139,6 +1270,7 @@ int pqdts_cuda_doproj(pqdts_ctx* c) {
   return guarded(c, [&] {
     pqdts::need_problem(*c);
     pqdts::project_rows(*c, c->X.p, nullptr, nullptr, c->X.p, 1);
+    pqdts::touch_x(*c);
     CK(cudaStreamSynchronize(c->st));
   });
 }
@@ -1152,6 +1284,7 @@ int pqdts_cuda_doproj2(pqdts_ctx* c, double* xmin) {
                                                                          (int64_t)M * N, c->maxr.p, M, N, 0,
                                                                          c->part2.p);
     pqdts::post_launch(*c);
+    pqdts::touch_x(*c);
     pqdts::reduce_to(*c, c->part2.p, gb, c->sc.p + pqdts::SC_TMP, 1, true, 0.0);
     pqdts::read_back(*c, c->sc.p + pqdts::SC_TMP, 1);
     if (xmin) *xmin = c->pin[0];

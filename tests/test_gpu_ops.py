@@ -181,3 +181,20 @@ def test_errors_are_codes(built):
             s.set_problem_coo(10, 3, 5, (np.array([0]), np.array([99]), np.array([1.0])), None, 0.0)
         with pytest.raises(pq.PqdtsError, match=r"\(D-1\)"):
             s.set_problem_coo(10, 3, 5, None, None, 0.0)
+
+
+@pytest.mark.parametrize("full", [True, False])
+def test_BF32_mixed_precision(built, cfg1, full):
+    """The mixed solver's FP32 Hessian product against the FP64 oracle:
+    FP32 values and accumulation, so relative to the product's scale the
+    error is bounded by a few FP32 ulps times sqrt(band width)."""
+    s, o = _pair(cfg1, precision=1)
+    X = _random_x(cfg1, 4)
+    m = None if full else _maxr(X)
+    s.set_space(full, m)
+    o.set_space(full, m)
+    V = np.asfortranarray(np.random.default_rng(5).standard_normal((cfg1.M, cfg1.N)))
+    H32 = s.BF32(V)
+    H64 = o.BF(V)
+    err = np.max(np.abs(H32 - H64)) / np.max(np.abs(H64))
+    assert err < 2e-5, err
