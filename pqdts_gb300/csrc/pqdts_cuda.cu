@@ -442,14 +442,17 @@ struct TransShape {
   int threads, C;
 };
 static TransShape trans_shape(int N) {
+  // fewest passes over the CSR row first (each pass re-reads it), then the
+  // fewest idle lanes, then the fewest columns per thread (more warps).
   TransShape best{32, 1};
-  int64_t best_waste = INT64_MAX;
+  int64_t best_passes = INT64_MAX, best_waste = INT64_MAX;
   for (int C : {1, 2, 4, 8})
     for (int t = 32; t <= 256; t += 32) {
       const int64_t per = (int64_t)t * C;
       const int64_t passes = (N + per - 1) / per;
       const int64_t waste = passes * per - N;
-      if (waste < best_waste) {
+      if (passes < best_passes || (passes == best_passes && waste < best_waste)) {
+        best_passes = passes;
         best_waste = waste;
         best = {t, C};
       }
@@ -688,9 +691,11 @@ static void line_search(Ctx& c, bool stage2, double& alpha, double& dlalpha) {
   double qa[kBatchLS] = {1.0}, qL[kBatchLS] = {L[2]}, qx[kBatchLS] = {xm[2]};
   int qlen = 1, qpos = 0;
   double next_a = 1.0 * 0.75;  // alpha of the probe after the queued ones
+  int next_batch = 2;  // probes per sweep after alpha = 1: 2, 4, 8, 8, ...
   for (int i = 1; i <= kMaxLS; ++i) {
     if (qpos == qlen) {
-      qlen = std::min(kBatchLS, kMaxLS - i + 1);
+      qlen = std::min(next_batch, kMaxLS - i + 1);
+      next_batch = std::min(kBatchLS, 2 * next_batch);
       for (int k = 0; k < qlen; ++k) {
         qa[k] = next_a;
         next_a = next_a * 0.75;
