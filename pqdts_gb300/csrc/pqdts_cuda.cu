@@ -300,7 +300,7 @@ static void setup_device(Ctx& c) {
   else c.aux.release();
   c.srow.alloc((size_t)kBatchLS * std::max(D, M));
   c.gcol.alloc((size_t)kBatchLS * N);
-  c.colbuf.alloc(N);
+  c.colbuf.alloc(2 * N);
   c.lred.alloc(kBatchLS);
   c.X.alloc(MN);
   c.G.alloc(MN);
@@ -356,7 +356,7 @@ static void objective_combine(Ctx& c, const double* Xs, int B) {
     post_launch(c);
     if (c.h.gam != 0) {
       k_colchain<1><<<dim3(cdiv(N, 32), B), 256, 0, c.st>>>(Xs, nullptr, (int64_t)M * N, M, N, c.h.gam, c.gcol.p,
-                                                           nullptr);
+                                                           nullptr, nullptr);
       post_launch(c);
       k_seqsum<<<1, 32, 0, c.st>>>(c.gcol.p, N, c.lred.p, c.lsout.p, B, nullptr);
       post_launch(c);
@@ -401,6 +401,8 @@ static void fetch_objectives(Ctx& c, int B, double* L) {
   for (int b = 0; b < B; ++b) L[b] = (c.h.gam != 0 && !c.exact) ? c.pin[b] + c.pin[kBatchLS + b] : c.pin[b];
 }
 
+// Max-column rebuild of the context's X (always a new version: across M
+// rows some row practically always moves by an ulp).
 static void rebuild_x(Ctx& c) {
   rebuild(c, c.X.p);
   touch_x(c);
@@ -501,7 +503,7 @@ static void op_dL(Ctx& c) {
 static void dot_dev(Ctx& c, const double* a, const double* b, double* out, const double* pred = nullptr) {
   const int M = (int)c.h.M, N = (int)c.h.N;
   if (c.exact) {
-    k_colchain<0><<<dim3(cdiv(N, 32), 1), 256, 0, c.st>>>(a, b, 0, M, N, 0.0, c.colbuf.p, pred);
+    k_colchain<0><<<dim3(cdiv(N, 32), 1), 256, 0, c.st>>>(a, b, 0, M, N, 0.0, c.colbuf.p, nullptr, pred);
     post_launch(c);
     k_seqsum<<<1, 32, 0, c.st>>>(c.colbuf.p, N, nullptr, out, 1, pred);
     post_launch(c);
@@ -512,6 +514,17 @@ static void dot_dev(Ctx& c, const double* a, const double* b, double* out, const
   k_dot_part<<<g, 256, 0, c.st>>>(total, a, b, c.part.p);
   post_launch(c);
   reduce_to(c, c.part.p, g, out, 1, false, 0.0, pred);
+}
+
+// Two pdots of the FP64 CG at once: a.b -> out_ab, a.a -> out_aa, where
+// out_aa = out_ab + ostride (two chains over one staged tile, two warps).
+static void dot2_exact(Ctx& c, const double* a, const double* b, double* out_ab, int ostride,
+                       const double* pred) {
+  const int M = (int)c.h.M, N = (int)c.h.N;
+  k_colchain<2><<<dim3(cdiv(N, 32), 1), 256, 0, c.st>>>(a, b, 0, M, N, 0.0, c.colbuf.p, c.colbuf.p + N, pred);
+  post_launch(c);
+  k_seqsum<<<1, 32, 0, c.st>>>(c.colbuf.p, N, nullptr, out_ab, 2, pred, ostride);
+  post_launch(c);
 }
 
 // Hessian-vector product of one precision: Hp = H p (BF, 246-342); masks the
@@ -551,8 +564,9 @@ static void cg_solve(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, double bdfa
   const bool exact = kF64 && c.exact;
   if (exact) {
     if constexpr (kF64) {
-      dot_dev(c, b.r.p, b.r.p, c.sc.p + SC_NORM);  // (-g).(-g) == g.g bit for bit
-      dot_dev(c, b.r.p, b.z.p, c.sc.p + SC_RZ);
+      // r.z -> SC_RZ and r.r -> SC_NORM ((-g).(-g) == g.g bit for bit)
+      static_assert(SC_NORM - SC_RZ == 3, "scalar layout");
+      dot2_exact(c, b.r.p, b.z.p, c.sc.p + SC_RZ, SC_NORM - SC_RZ, nullptr);
     }
   } else {
     reduce_to(c, c.part.p, g, c.sc.p + SC_NORM);
@@ -600,8 +614,8 @@ static void cg_solve(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, double bdfa
       post_launch(c);
       if (exact) {
         if constexpr (kF64) {
-          dot_dev(c, b.r.p, b.z.p, c.sc.p + SC_RZ, c.sc.p);
-          dot_dev(c, b.r.p, b.r.p, c.sc.p + SC_RR, c.sc.p);
+          static_assert(SC_RR - SC_RZ == 1, "scalar layout");
+          dot2_exact(c, b.r.p, b.z.p, c.sc.p + SC_RZ, 1, c.sc.p);
         }
       } else {
         reduce_to(c, c.part.p, g, c.sc.p + SC_RZ, 1, false, 0.0, c.sc.p);
