@@ -1,0 +1,163 @@
+! pqdts_cuda_mod -- iso_c_binding interface of libpqdts_cuda.so for a Fortran
+! host such as program pqdts (pqdts.f90).  Declarations mirror
+! include/pqdts_cuda.h one to one; arrays are passed as in the reference
+! (X(M,N) and P(N,D) column-major, real64), indices 0-based, every function
+! returns 0 on success or a negative error code.
+!
+! Build (needs a Fortran compiler):
+!   gfortran -c pqdts_cuda_mod.f90
+!   gfortran ... pqdts.f90 pqdts_cuda_mod.o -L<dir> -lpqdts_cuda -Wl,-rpath,<dir>
+module pqdts_cuda_mod
+  use iso_c_binding, only: c_int32_t, c_int64_t, c_double, c_ptr, c_funptr, c_char
+  implicit none
+
+  integer(c_int32_t), parameter :: PQDTS_FP64 = 0, PQDTS_MIXED = 1
+
+  interface
+    integer(c_int32_t) function pqdts_cuda_create(device, ctx) bind(C, name="pqdts_cuda_create")
+      import :: c_int32_t, c_ptr
+      integer(c_int32_t), value :: device
+      type(c_ptr) :: ctx
+    end function
+
+    integer(c_int32_t) function pqdts_cuda_destroy(ctx) bind(C, name="pqdts_cuda_destroy")
+      import :: c_int32_t, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+
+    integer(c_int32_t) function pqdts_cuda_last_error(ctx, buf, len) bind(C, name="pqdts_cuda_last_error")
+      import :: c_int32_t, c_int64_t, c_ptr, c_char
+      type(c_ptr), value :: ctx
+      character(kind=c_char) :: buf(*)
+      integer(c_int64_t), value :: len
+    end function
+
+    integer(c_int32_t) function pqdts_cuda_set_verbose(ctx, verbose) bind(C, name="pqdts_cuda_set_verbose")
+      import :: c_int32_t, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: verbose
+    end function
+
+    ! replaces read_sparse_from_python + band build + P assembly (pqdts.f90:1318-1538)
+    integer(c_int32_t) function pqdts_cuda_set_problem_coo(ctx, M, N, D, nnzF, F_row, F_col, F_val, &
+                                                           nnzP, P_row, P_col, P_val, gamma, precision) &
+      bind(C, name="pqdts_cuda_set_problem_coo")
+      import :: c_int32_t, c_int64_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int64_t), value :: M, N, D, nnzF, nnzP
+      integer(c_int32_t) :: F_row(*), F_col(*), P_row(*), P_col(*)
+      real(c_double) :: F_val(*), P_val(*)
+      real(c_double), value :: gamma
+      integer(c_int32_t), value :: precision
+    end function
+
+    ! replaces the Frows bands + dense P (pqdts.f90:77-83, 1528)
+    integer(c_int32_t) function pqdts_cuda_set_problem(ctx, M, N, D, band_lo, band_hi, band_vals, P_ND, &
+                                                       gamma, precision) bind(C, name="pqdts_cuda_set_problem")
+      import :: c_int32_t, c_int64_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int64_t), value :: M, N, D
+      integer(c_int64_t) :: band_lo(*), band_hi(*)
+      real(c_double) :: band_vals(*), P_ND(*)
+      real(c_double), value :: gamma
+      integer(c_int32_t), value :: precision
+    end function
+
+    integer(c_int32_t) function pqdts_cuda_set_x(ctx, X) bind(C, name="pqdts_cuda_set_x")
+      import :: c_int32_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      real(c_double) :: X(*)
+    end function
+
+    integer(c_int32_t) function pqdts_cuda_get_x(ctx, X) bind(C, name="pqdts_cuda_get_x")
+      import :: c_int32_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      real(c_double) :: X(*)
+    end function
+
+    integer(c_int32_t) function pqdts_cuda_set_space(ctx, fullspace, maxr) bind(C, name="pqdts_cuda_set_space")
+      import :: c_int32_t, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: fullspace
+      integer(c_int32_t) :: maxr(*)
+    end function
+
+    ! subroutine L(X, val), pqdts.f90:917
+    integer(c_int32_t) function pqdts_cuda_L(ctx, val) bind(C, name="pqdts_cuda_L")
+      import :: c_int32_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      real(c_double) :: val
+    end function
+
+    ! subroutine dL(X, dLdX), pqdts.f90:975
+    integer(c_int32_t) function pqdts_cuda_dL(ctx, G) bind(C, name="pqdts_cuda_dL")
+      import :: c_int32_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      real(c_double) :: G(*)
+    end function
+
+    ! subroutine BF(dd, BX), pqdts.f90:246
+    integer(c_int32_t) function pqdts_cuda_BF(ctx, V, HV) bind(C, name="pqdts_cuda_BF")
+      import :: c_int32_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      real(c_double) :: V(*), HV(*)
+    end function
+
+    ! subroutine Bdiag(BD), pqdts.f90:208
+    integer(c_int32_t) function pqdts_cuda_Bdiag(ctx, BD) bind(C, name="pqdts_cuda_Bdiag")
+      import :: c_int32_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      real(c_double) :: BD(*)
+    end function
+
+    ! subroutine doproj(X), pqdts.f90:1120
+    integer(c_int32_t) function pqdts_cuda_doproj(ctx) bind(C, name="pqdts_cuda_doproj")
+      import :: c_int32_t, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+
+    ! subroutine doproj2(X, xmin), pqdts.f90:1142
+    integer(c_int32_t) function pqdts_cuda_doproj2(ctx, xmin) bind(C, name="pqdts_cuda_doproj2")
+      import :: c_int32_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      real(c_double) :: xmin
+    end function
+
+    ! subroutine conv_test(X, dLdX, tprint, conv), pqdts.f90:1034
+    integer(c_int32_t) function pqdts_cuda_conv_test(ctx, conv) bind(C, name="pqdts_cuda_conv_test")
+      import :: c_int32_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      real(c_double) :: conv
+    end function
+
+    ! simplexproj_condat_(y, x, len), condat_simplexproj.c:60
+    integer(c_int32_t) function pqdts_cuda_simplexproj(ctx, y, x, len, rows) bind(C, name="pqdts_cuda_simplexproj")
+      import :: c_int32_t, c_int64_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      real(c_double) :: y(*), x(*)
+      integer(c_int64_t), value :: len, rows
+    end function
+
+    ! one stage of the loop at pqdts.f90:1927-2166
+    integer(c_int32_t) function pqdts_cuda_run_stage(ctx, mode, oiter, maxiiter, conv_thres, output, stats) &
+      bind(C, name="pqdts_cuda_run_stage")
+      import :: c_int32_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: mode, oiter, maxiiter, output
+      real(c_double), value :: conv_thres
+      real(c_double) :: stats(8)
+    end function
+
+    ! the minimisation of program pqdts, pqdts.f90:1908-2167
+    integer(c_int32_t) function pqdts_cuda_solve(ctx, mode, maxiiter, conv_thres, start_stage, output, &
+                                                 stage_cb, user, stats) bind(C, name="pqdts_cuda_solve")
+      import :: c_int32_t, c_double, c_ptr, c_funptr
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: mode, maxiiter, start_stage, output
+      real(c_double), value :: conv_thres
+      type(c_funptr), value :: stage_cb
+      type(c_ptr), value :: user
+      real(c_double) :: stats(8)
+    end function
+  end interface
+end module pqdts_cuda_mod
