@@ -112,6 +112,24 @@ int pqdts_cuda_conv_test(pqdts_ctx* ctx, double* conv);            /* conv_test,
  * pqdts.f90:1133). */
 int pqdts_cuda_simplexproj(pqdts_ctx* ctx, const double* y, double* x, int64_t len, int64_t rows);
 
+/* The same projection for callers that cannot allocate device memory, e.g.
+ * a host that owns all device memory through its own pool and forbids other
+ * allocations after start-up.  No counterpart in the reference.  Needs no
+ * context and allocates nothing: d_y and d_x (rows*len doubles each, may
+ * alias) are the caller's device buffers, the kernel's scratch is a fixed
+ * static device array of PQDTS_NOALLOC_SCRATCH doubles (8 MiB) that every
+ * GPU loading this library holds until the process exits.  rows*len above
+ * that capacity is rejected with PQDTS_E_ARG and a message on stderr.
+ * Runs asynchronously on `stream` (a cudaStream_t; NULL = legacy default
+ * stream) of the current device.  The first call on a device looks up the
+ * scratch address on that device; make that first call before any stream
+ * capture.  All calls share the one scratch array (its contents are fully
+ * rewritten before use, nothing needs clearing), so calls whose kernels can
+ * overlap on the GPU -- different streams, different host threads -- race
+ * and must be serialised by the caller. */
+enum { PQDTS_NOALLOC_SCRATCH = 1 << 20 };
+int pqdts_cuda_simplexproj_noalloc(const double* d_y, double* d_x, int64_t len, int64_t rows, void* stream);
+
 /* Solve statistics filled by the solve entry points (may be null):
  * [0] final L  [1] final conv  [2] ||der||  [3] outer iterations
  * [4] CG iterations  [5] line-search L evaluations  [6] FP64 refinement

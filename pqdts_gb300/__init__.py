@@ -70,6 +70,7 @@ def lib():
         "pqdts_cuda_doproj2": [p, C.POINTER(d)],
         "pqdts_cuda_conv_test": [p, C.POINTER(d)],
         "pqdts_cuda_simplexproj": [p, p, p, i64, i64],
+        "pqdts_cuda_simplexproj_noalloc": [p, p, i64, i64, p],
         "pqdts_cuda_run_stage": [p, i32, i32, i32, d, i32, p],
         "pqdts_cuda_solve": [p, i32, i32, d, i32, i32, p, p, p],
         "pqdts_cuda_timer": [p, C.c_char_p, C.POINTER(d), C.POINTER(i64)],

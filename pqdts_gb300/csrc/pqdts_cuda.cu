@@ -229,6 +229,14 @@ namespace pqdts {
 
 using Ctx = pqdts_ctx;
 
+// Scratch of pqdts_cuda_simplexproj_noalloc: Condat's per-row working lists.
+// In host code this name is only a stand-in for the symbol; the device
+// address comes from cudaGetSymbolAddress, once per device.
+static __device__ __align__(256) double g_noalloc_scratch[PQDTS_NOALLOC_SCRATCH];
+constexpr int kMaxDevices = 64;
+static std::mutex g_noalloc_mu;
+static double* g_noalloc_ptr[kMaxDevices] = {};
+
 static DevBands bands_of(Ctx& c) {
   DevBands b;
   b.M = (int)c.h.M;
@@ -1331,6 +1339,48 @@ int pqdts_cuda_simplexproj(pqdts_ctx* c, const double* y, double* x, int64_t len
     CK(cudaMemcpyAsync(x, d.p, len * rows * 8, cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
   });
+}
+
+int pqdts_cuda_simplexproj_noalloc(const double* d_y, double* d_x, int64_t len, int64_t rows, void* stream) {
+  if (!d_y || !d_x || len <= 0 || rows <= 0) {
+    fprintf(stderr, "pqdts_cuda_simplexproj_noalloc: null buffer or non-positive size\n");
+    return PQDTS_E_ARG;
+  }
+  if (len > PQDTS_NOALLOC_SCRATCH / rows || len * rows > PQDTS_NOALLOC_SCRATCH) {
+    fprintf(stderr,
+            "pqdts_cuda_simplexproj_noalloc: rows*len = %lld*%lld exceeds the scratch capacity of %d values\n",
+            (long long)rows, (long long)len, (int)PQDTS_NOALLOC_SCRATCH);
+    return PQDTS_E_ARG;
+  }
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= pqdts::kMaxDevices) {
+    fprintf(stderr, "pqdts_cuda_simplexproj_noalloc: no usable current device: %s\n", cudaGetErrorString(e));
+    return PQDTS_E_CUDA;
+  }
+  double* scratch = nullptr;
+  {
+    // set-up once per device, with that device current: the scratch's device address
+    std::lock_guard<std::mutex> g(pqdts::g_noalloc_mu);
+    if (pqdts::g_noalloc_ptr[dev] == nullptr) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, pqdts::g_noalloc_scratch);
+      if (e != cudaSuccess || p == nullptr) {
+        fprintf(stderr, "pqdts_cuda_simplexproj_noalloc: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+        return PQDTS_E_CUDA;
+      }
+      pqdts::g_noalloc_ptr[dev] = static_cast<double*>(p);
+    }
+    scratch = pqdts::g_noalloc_ptr[dev];
+  }
+  pqdts::k_condat<<<dim3(pqdts::cdiv(rows, pqdts::kRowThreads), 1), pqdts::kRowThreads, 0, (cudaStream_t)stream>>>(
+      d_y, nullptr, nullptr, d_x, scratch, 0, (int)rows, (int)len);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    fprintf(stderr, "pqdts_cuda_simplexproj_noalloc: launch failed: %s\n", cudaGetErrorString(e));
+    return PQDTS_E_CUDA;
+  }
+  return PQDTS_OK;
 }
 
 int pqdts_cuda_run_stage(pqdts_ctx* c, int32_t mode, int32_t oiter, int32_t maxiiter, double conv_thres,
