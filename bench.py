@@ -473,6 +473,59 @@ def run_profile_case(case):
     return 0
 
 
+def run_workload(name, args):
+    """Secondary measurements (one JSON line each, not the bench line):
+      batch   -- 64 uneven instances (8 base detectors x 8 resampled P with a
+                 gamma sweep), solved one after another through one context
+                 vs. all through pqdts_cuda_solve_batch (concurrent contexts),
+                 FP64 and mixed, reference stopping rule conv < 1e-6;
+      config3 -- M=10000, N=1000, D=20000: FP64 vs mixed seconds per outer
+                 iteration over the first iterations of each stage."""
+    import numpy as np
+
+    import pqdts_gb300 as pq
+    from pqdts_gb300 import synth
+
+    if name == "batch":
+        insts = synth.make_batch(seed=0)
+        out = {"workload": "batch of %d instances" % len(insts),
+               "sizes": {"M": [i.M for i in insts[::8]], "N": [i.N for i in insts[::8]]}}
+        for prec, tag in ((pq.FP64, "fp64"), (pq.MIXED, "mixed")):
+            t0 = time.perf_counter()
+            Ls = []
+            with pq.Solver(0) as s:
+                for inst in insts:
+                    s.set_instance(inst, prec)
+                    Ls.append(s.solve(mode=2, maxiter=args.batch_maxiter, eps=EPS)["L"])
+            t_seq = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            Xs, st = pq.solve_batch(insts, precision=prec, maxiter=args.batch_maxiter, eps=EPS)
+            t_bat = time.perf_counter() - t0
+            same = all(a == b["L"] for a, b in zip(Ls, st))
+            out[tag] = {"sequential_s": t_seq, "batched_s": t_bat, "speedup": t_seq / t_bat,
+                        "identical_objectives": same, "outer_total": sum(x["outer"] for x in st),
+                        "cg_total": sum(x["cg"] for x in st)}
+        print(json.dumps(out))
+        return 0
+    if name == "config3":
+        inst = synth.make_config(3, seed=0)
+        out = {"workload": "M=10000 N=1000 D=20000", "nnz_F": inst.nnz}
+        for prec, tag in ((pq.FP64, "fp64"), (pq.MIXED, "mixed")):
+            with pq.Solver(0) as s:
+                s.set_instance(inst, prec)
+                s.init_x()
+                t0 = time.perf_counter()
+                st = s.solve(mode=2, maxiter=args.config3_iters, eps=EPS)
+                el = time.perf_counter() - t0
+                bf = s.timer("BF")
+            out[tag] = {"seconds": el, "outer": st["outer"], "cg": st["cg"], "s_per_outer": el / max(1, st["outer"]),
+                        "L": st["L"], "bf_seconds": bf[0], "bf_calls": bf[1],
+                        "bf_tflops": 2 * 2.0 * inst.nnz * inst.N * st["cg"] / bf[0] / 1e12 if bf[0] else None}
+        print(json.dumps(out))
+        return 0
+    raise SystemExit("unknown workload " + name)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -487,7 +540,13 @@ def main():
     ap.add_argument("--ref-sample-iters", type=int, default=3)
     ap.add_argument("--profile-case", choices=["fp64", "mixed", "solve64", "solvemix"], default=None,
                     help="launches of the workload for ncu (see run_profile_case)")
+    ap.add_argument("--workload", choices=["batch", "config3"], default=None,
+                    help="secondary measurement instead of the bench line")
+    ap.add_argument("--batch-maxiter", type=int, default=200)
+    ap.add_argument("--config3-iters", type=int, default=3)
     args = ap.parse_args()
+    if args.workload:
+        return run_workload(args.workload, args)
     if args.profile_case:
         return run_profile_case(args.profile_case)
     if args.warmup < 3:

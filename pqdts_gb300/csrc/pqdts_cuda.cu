@@ -197,7 +197,9 @@ struct pqdts_ctx {
   pqdts::DBuf<int32_t> flo, fw, tidx;
   pqdts::DBuf<int64_t> foff, tptr;
   pqdts::DBuf<double> fval, tval, bdiag, P;
-  pqdts::DBuf<float> fval32, tval32;
+  pqdts::DBuf<float> fval32, tval32, tbval32, rsq32;
+  pqdts::DBuf<int32_t> tlo, tw;
+  pqdts::DBuf<int64_t> toff;
   // iterate and work arrays
   pqdts::DBuf<double> X, G, Xc, R, sn64;
   pqdts::DBuf<int8_t> ik;
@@ -219,7 +221,7 @@ struct pqdts_ctx {
   bool refine = false;  // mixed precision: FP64 CG from now on
   double target_L = 0.0;  // optional objective stopping rule (0 = off)
   // version of X, bumped on every write; results keyed on it are reused
-  int64_t xver = 0, R_ver = -1, G_ver = -1, L_ver = -1;
+  int64_t xver = 0, R_ver = -1, G_ver = -1, L_ver = -1, rebuilt_ver = -1;
   bool G_full = true;
   double L_cache = 0.0;
   bool target_hit = false;
@@ -294,10 +296,19 @@ static void setup_device(Ctx& c) {
     c.fval32.upload(f32.data(), f32.size(), c.st, &c.h2d);
     std::vector<float> t32(h.tval.begin(), h.tval.end());
     c.tval32.upload(t32.data(), t32.size(), c.st, &c.h2d);
+    transposed_bands(h);
+    c.tlo.upload(h.tlo.data(), h.tlo.size(), c.st, &c.h2d);
+    c.tw.upload(h.tw.data(), h.tw.size(), c.st, &c.h2d);
+    c.toff.upload(h.toff.data(), h.toff.size(), c.st, &c.h2d);
+    std::vector<float> tb32(h.tbval.begin(), h.tbval.end());
+    c.tbval32.upload(tb32.data(), tb32.size(), c.st, &c.h2d);
+    c.rsq32.alloc(M);
     c.cg32.alloc(MN, M, D * N);
+    CK(cudaStreamSynchronize(c.st));  // host staging vectors go out of scope
   } else {
     c.fval32.release();
     c.tval32.release();
+    c.tbval32.release();
   }
   c.cg64.alloc(MN, M, D * N);
   c.exact = (c.precision == PQDTS_FP64);
@@ -330,7 +341,7 @@ static void setup_device(Ctx& c) {
   // Initial X = 1/N (pqdts.f90:1834-1838) and maxr from the seeded stream.
   k_fill<<<elem_grid(MN), 256, 0, c.st>>>(MN, 1.0 / (double)N, c.X.p);
   post_launch(c);
-  c.R_ver = c.G_ver = c.L_ver = -1;
+  c.R_ver = c.G_ver = c.L_ver = c.rebuilt_ver = -1;
   touch_x(c);
   CK(cudaMemcpyAsync(c.maxr.p, c.h_maxr.data(), M * 4, cudaMemcpyHostToDevice, c.st));
   c.h2d += M * 4;
@@ -409,11 +420,16 @@ static void fetch_objectives(Ctx& c, int B, double* L) {
   for (int b = 0; b < B; ++b) L[b] = (c.h.gam != 0 && !c.exact) ? c.pin[b] + c.pin[kBatchLS + b] : c.pin[b];
 }
 
-// Max-column rebuild of the context's X (always a new version: across M
-// rows some row practically always moves by an ulp).
+// Max-column rebuild of the context's X.  FP64 path: always a new version
+// of X (across M rows some row practically always moves by an ulp, and the
+// trajectory must stay bit-exact).  Mixed path: re-applying the rebuild to
+// an X that is already consistent with maxr only moves values by ulps, so
+// results computed for that X stay in use.
 static void rebuild_x(Ctx& c) {
   rebuild(c, c.X.p);
+  if (!c.exact && c.rebuilt_ver == c.xver) return;
   touch_x(c);
+  c.rebuilt_ver = c.xver;
 }
 
 // R = 2*(O - P) with O = F.X for the context's X, unless R already holds it
@@ -551,6 +567,113 @@ static void hvp(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, const int8_t* ik
                         (T)(2.0 * c.h.gam), ik, b.Hp.p, with_dot ? b.p.p : nullptr, with_dot ? c.part.p : nullptr,
                         pred);
   if (with_dot) reduce_to(c, c.part.p, M, c.sc.p + SC_V2, 1, false, 0.0, pred);
+}
+
+// Mixed precision Hessian product Hp = H p in FP32 with the tiled band
+// products (F.V then F^T.(2O)) and the row epilogue; p.Hp -> sc[SC_V2].
+// Out (R x N) = scale * Band (R rows) . In, with the largest tile that
+// still gives at least two CTAs per SM (small problems need more, smaller
+// tiles to fill the GPU).
+static void band_gemm32(Ctx& c, const int32_t* lo, const int32_t* w, const int64_t* off, const float* vals,
+                        const float* In, int R, int N, float scale, float* Out, const double* pred) {
+  const int64_t want = 2 * 152;
+  auto ctas = [&](int tr, int tn) { return (int64_t)cdiv(R, tr) * cdiv(N, tn); };
+  if (ctas(64, 64) >= want) {
+    k_band_gemm32<64, 64><<<dim3(cdiv(N, 64), cdiv(R, 64)), 256, 0, c.st>>>(lo, w, off, vals, In, R, N, scale, Out, pred);
+  } else if (ctas(64, 32) >= want) {
+    k_band_gemm32<64, 32><<<dim3(cdiv(N, 32), cdiv(R, 64)), 128, 0, c.st>>>(lo, w, off, vals, In, R, N, scale, Out, pred);
+  } else {
+    k_band_gemm32<32, 32><<<dim3(cdiv(N, 32), cdiv(R, 32)), 64, 0, c.st>>>(lo, w, off, vals, In, R, N, scale, Out, pred);
+  }
+  post_launch(c);
+}
+
+// Mixed precision Hessian product Hp = H p in FP32 with the tiled band
+// products (F.V then F^T.(2O)) and the row epilogue; p.Hp -> sc[SC_V2].
+static void hvp32(Ctx& c, CGBufs<float>& b, const int8_t* ik, bool with_dot, const double* pred) {
+  const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
+  const float* src = c.fullspace ? b.p.p : b.V.p;
+  band_gemm32(c, c.flo.p, c.fw.p, c.foff.p, c.fval32.p, src, D, N, 2.0f, b.R2.p, pred);
+  band_gemm32(c, c.tlo.p, c.tw.p, c.toff.p, c.tbval32.p, b.R2.p, M, N, 1.0f, b.Hp.p, pred);
+  const int tb = std::min(256, std::max(32, cdiv(N, 32) * 32));
+  k_hvp_epi32<<<M, tb, 0, c.st>>>(b.Hp.p, b.p.p, c.fullspace ? nullptr : b.rs.p, c.maxr.p, c.fullspace ? 0 : 1,
+                                  (float)(2.0 * c.h.gam), ik, M, N, b.Hp.p, with_dot ? c.part.p : nullptr, pred);
+  post_launch(c);
+  if (with_dot) reduce_to(c, c.part.p, M, c.sc.p + SC_V2, 1, false, 0.0, pred);
+}
+
+// The truncated-Newton PCG (2007-2090) in FP32 (mixed precision): the same
+// recurrence and exit test as cg_solve, tiled FP32 products, warp-per-row
+// lift, FP32 vectors with FP64 block sums.
+static void cg_solve32(Ctx& c, double bdfac) {
+  const int M = (int)c.h.M, N = (int)c.h.N;
+  const int64_t MN = (int64_t)M * N;
+  const int g = elem_grid(MN);
+  CGBufs<float>& b = c.cg32;
+  require(c.tbval32.p, "F^T band values (FP32)");
+  Scope s(c.timers, "CG");
+  k_cg_init<float><<<g, 256, 0, c.st>>>(c.X.p, c.G.p, c.bdiag.p, bdfac, kActiveTol, M, N, c.ik.p, b.r.p, b.z.p, b.p.p,
+                                        b.sn.p, c.part.p, c.part2.p, c.ipart.p);
+  post_launch(c);
+  reduce_to(c, c.part.p, g, c.sc.p + SC_NORM);
+  reduce_to(c, c.part2.p, g, c.sc.p + SC_RZ);
+  k_sum_i<<<1, 256, 0, c.st>>>(c.ipart.p, g, c.icount.p);
+  post_launch(c);
+  k_cg_scalars0<<<1, 1, 0, c.st>>>(c.sc.p);
+  post_launch(c);
+  k_rsqrt_diag<<<cdiv(M, 256), 256, 0, c.st>>>(c.bdiag.p, bdfac, M, c.rsq32.p);
+  post_launch(c);
+  if (c.verbose) {
+    long long nact = 0;
+    CK(cudaMemcpyAsync(&nact, c.icount.p, sizeof(long long), cudaMemcpyDeviceToHost, c.st));
+    CK(cudaStreamSynchronize(c.st));
+    ListLine l;
+    l.s("positivity constraints").i8(nact).s("active of").i8(MN).r8((double)nact / (double)MN).print();
+  }
+  const int lift_blocks = cdiv((int64_t)M * 32, 256);
+  int queued = 0, chunk = 4, done_iters = 0;
+  for (;;) {
+    for (int k = 0; k < chunk && queued < kMaxCG; ++k, ++queued) {
+      if (c.fullspace) {
+        if (queued > 0) {
+          k_cg_pupdate<float><<<g, 256, 0, c.st>>>(c.sc.p, MN, b.p.p, b.z.p);
+          post_launch(c);
+        }
+      } else {
+        k_cg_lift32<<<lift_blocks, 256, 0, c.st>>>(queued > 0 ? c.sc.p : nullptr, queued > 0 ? 1 : 0, M, N, b.p.p,
+                                                   b.z.p, c.maxr.p, b.V.p, b.rs.p);
+        post_launch(c);
+      }
+      {
+        Scope sb(c.timers, "BF");
+        hvp32(c, b, c.ik.p, true, c.sc.p);
+      }
+      k_cg_step32<<<g, 256, 0, c.st>>>(c.sc.p, c.rsq32.p, M, N, b.p.p, b.Hp.p, b.sn.p, b.r.p, b.z.p, c.part.p,
+                                       c.part2.p);
+      post_launch(c);
+      reduce_to(c, c.part.p, g, c.sc.p + SC_RZ, 1, false, 0.0, c.sc.p);
+      reduce_to(c, c.part2.p, g, c.sc.p + SC_RR, 1, false, 0.0, c.sc.p);
+      k_cg_scalars1<<<1, 1, 0, c.st>>>(c.sc.p, c.cglog.p, kMaxCG);
+      post_launch(c);
+    }
+    read_back(c, c.sc.p, SC_NSC);
+    if (c.pin[SC_DONE] != 0.0 || queued >= kMaxCG) {
+      done_iters = (int)c.pin[SC_ITER];
+      break;
+    }
+    chunk = 8;
+  }
+  c.n_cg += done_iters;
+  if (c.verbose) {
+    std::vector<double> lg(4 * kMaxCG);
+    CK(cudaMemcpyAsync(lg.data(), c.cglog.p, lg.size() * 8, cudaMemcpyDeviceToHost, c.st));
+    CK(cudaStreamSynchronize(c.st));
+    for (int j = 0; j < done_iters; ++j) {
+      ListLine l;
+      l.s("newton-pcg").i4(j + 1).s("sqrt(b2)=").r8(lg[4 * j]).s("eps=").r8(lg[4 * j + 1]).s("b1=").r8(lg[4 * j + 2]);
+      l.s("v2=").r8(lg[4 * j + 3]).print();
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -821,7 +944,7 @@ static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
     op_dL(c);
     const double bdfac = c.fullspace ? 1.0 : 2.0;
     const bool fp32 = (c.precision == PQDTS_MIXED) && !c.refine;
-    if (fp32) cg_solve<float>(c, c.cg32, c.fval32.p, c.tval32.p, bdfac, nullptr);
+    if (fp32) cg_solve32(c, bdfac);
     else cg_solve<double>(c, c.cg64, c.fval.p, c.tval.p, bdfac, nullptr);
     if (c.precision == PQDTS_MIXED && c.refine) c.n_refine++;
     op_dL(c);
@@ -852,6 +975,7 @@ static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
                                                          c.part2.p);
     post_launch(c);
     touch_x(c);
+    c.rebuilt_ver = c.xver;  // doproj2 ends with the max-column rebuild
     reduce_to(c, c.part2.p, gb, c.sc.p + SC_TMP, 1, true, 0.0);
     read_back(c, c.sc.p + SC_TMP, 1);
     st.xmin = c.pin[0];
@@ -1270,11 +1394,11 @@ int pqdts_cuda_BF32(pqdts_ctx* c, const double* V, double* HV) {
     CK(cudaMemcpyAsync(b.p.p, rm.data(), rm.size() * 4, cudaMemcpyHostToDevice, c->st));
     c->h2d += (int64_t)rm.size() * 4;
     if (!c->fullspace) {
-      pqdts::k_cg_lift<float><<<pqdts::cdiv(M, pqdts::kRowThreads), pqdts::kRowThreads, 0, c->st>>>(
-          nullptr, 0, (int)M, (int)N, b.p.p, b.z.p, c->maxr.p, b.V.p, b.rs.p);
+      pqdts::k_cg_lift32<<<pqdts::cdiv(M * 32, 256), 256, 0, c->st>>>(nullptr, 0, (int)M, (int)N, b.p.p, b.z.p,
+                                                                     c->maxr.p, b.V.p, b.rs.p);
       pqdts::post_launch(*c);
     }
-    pqdts::hvp<float>(*c, b, c->fval32.p, c->tval32.p, nullptr, false);
+    pqdts::hvp32(*c, b, nullptr, false, nullptr);
     CK(cudaMemcpyAsync(rm.data(), b.Hp.p, rm.size() * 4, cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     c->d2h += (int64_t)rm.size() * 4;

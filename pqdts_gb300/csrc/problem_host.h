@@ -24,6 +24,11 @@ struct HostProblem {
   std::vector<int32_t> tidx;
   std::vector<double> tval;
   std::vector<double> bdiag;     // full-space Hessian diagonal, one value per row i
+  // F^T as dense bands over d (zero filled where column i is not in row d's
+  // band): the mixed-precision tiled product's operand.
+  std::vector<int32_t> tlo, tw;
+  std::vector<int64_t> toff;
+  std::vector<double> tbval;
   int64_t nnz() const { return (int64_t)fval.size(); }
 };
 
@@ -179,6 +184,26 @@ inline void finish_problem(HostProblem& h) {
     for (int64_t j = 0; j + 1 < h.M; ++j) h.bdiag[j] = h.bdiag[j] + 2.0 * h.gam;
     for (int64_t j = 1; j < h.M; ++j) h.bdiag[j] = h.bdiag[j] + 2.0 * h.gam;
   }
+}
+
+// Band form of F^T from the transposed CSR: row i spans d = tidx[first] ..
+// tidx[last]; entries of d outside that row's CSR stay zero.
+inline void transposed_bands(HostProblem& h) {
+  h.tlo.assign(h.M, -1);
+  h.tw.assign(h.M, 0);
+  h.toff.assign(h.M, 0);
+  int64_t tot = 0;
+  for (int64_t i = 0; i < h.M; ++i) {
+    h.toff[i] = tot;
+    if (h.tptr[i + 1] > h.tptr[i]) {
+      h.tlo[i] = h.tidx[h.tptr[i]];
+      h.tw[i] = h.tidx[h.tptr[i + 1] - 1] - h.tlo[i] + 1;
+      tot += h.tw[i];
+    }
+  }
+  h.tbval.assign(tot, 0.0);
+  for (int64_t i = 0; i < h.M; ++i)
+    for (int64_t e = h.tptr[i]; e < h.tptr[i + 1]; ++e) h.tbval[h.toff[i] + h.tidx[e] - h.tlo[i]] = h.tval[e];
 }
 
 // Initial maxr from the seeded random X (pqdts.f90:1565-1575); call after P.
