@@ -210,6 +210,10 @@ struct pqdts_ctx {
   // reference-order reductions (FP64 path): residual stack, Condat scratch,
   // per-row / per-column chain results
   pqdts::DBuf<double> Rst, aux, srow, gcol, colbuf, lred;
+  // mixed-precision line search: alpha = 0 candidate, its residual (FP32),
+  // candidate differences and their banded products (FP32)
+  pqdts::DBuf<double> x0c;
+  pqdts::DBuf<float> r0_32, d32, fdx32;
   bool exact = true;  // FP64: every reduction in the oracle's order
   pqdts::DBuf<int> ipart;
   pqdts::DBuf<long long> icount;
@@ -304,6 +308,10 @@ static void setup_device(Ctx& c) {
     c.tbval32.upload(tb32.data(), tb32.size(), c.st, &c.h2d);
     c.rsq32.alloc(M);
     c.cg32.alloc(MN, M, D * N);
+    c.x0c.alloc(MN);
+    c.r0_32.alloc(D * N);
+    c.d32.alloc((size_t)kBatchLS * MN);
+    c.fdx32.alloc((size_t)kBatchLS * D * N);
     CK(cudaStreamSynchronize(c.st));  // host staging vectors go out of scope
   } else {
     c.fval32.release();
@@ -821,51 +829,168 @@ static void eval_candidates(Ctx& c, const double* al, int B, bool stage2, double
 // full space, Lalpha_min2 (394-438) in the reduced space.  Step lengths are
 // evaluated kBatchLS at a time; the reference's sequential accept rule is
 // then applied to them in order, so the chosen alpha is the same.
+// State of the reference's sequential backtracking (374-388, 420-435,
+// 466-480): probes alpha_i = 0.75^(i-1), the smallest L seen (feasible in
+// stage 2), stop at the first probe with sufficient decrease.
+struct LSState {
+  double L0, df, lm = kHuge, alphamin = 0.0, next_a = 1.0;
+  int i = 1;  // index of the next probe
+  bool done = false;
+};
+
+// One probe's decision; returns true when the search stops at it.
+static bool ls_take(Ctx& c, LSState& ls, bool stage2, double alpha_i, double Lp, double xmin) {
+  const bool better = stage2 ? (Lp < ls.lm && xmin >= -kFeasTol) : (Lp < ls.lm);
+  if (better) {
+    ls.lm = Lp;
+    ls.alphamin = alpha_i;
+  }
+  if (c.verbose) {
+    ListLine l;
+    l.s("line search").i8(ls.i).s("L=").r8(Lp).s("alpha=").r8(alpha_i).s("df(0)=").r8(ls.df);
+    if (stage2) l.s("min(X)=").r8(xmin);
+    l.print();
+  }
+  ls.i++;
+  const double armijo = std::fma(0.1 * alpha_i, ls.df, ls.L0);
+  const bool shrink = stage2 ? (Lp > armijo || xmin < -kFeasTol) : (Lp > armijo);
+  if (!shrink) ls.done = true;
+  return ls.done;
+}
+
+// The rest of the sequence with FP64 objectives, first_batch probes at a
+// time then doubling (the reference's rule applied to each batch in order).
+static void ls_continue_fp64(Ctx& c, LSState& ls, bool stage2, int first_batch) {
+  double qa[kBatchLS], qL[kBatchLS], qx[kBatchLS];
+  int nb = first_batch;
+  while (!ls.done && ls.i <= kMaxLS) {
+    const int qlen = std::min(nb, kMaxLS - ls.i + 1);
+    nb = std::min(kBatchLS, 2 * nb);
+    for (int k = 0; k < qlen; ++k) {
+      qa[k] = ls.next_a;
+      ls.next_a = ls.next_a * 0.75;
+    }
+    eval_candidates(c, qa, qlen, stage2, qL, qx);
+    for (int k = 0; k < qlen && !ls.done; ++k) ls_take(c, ls, stage2, qa[k], qL[k], qx[k]);
+  }
+}
+
+// Projected backtracking line search: Lalpha_min_auglag (440-483) in the
+// full space, Lalpha_min2 (394-438) in the reduced space.  FP64 path: every
+// probe's objective in FP64, evaluated in batches (3, 2, 4, 8, ...), the
+// reference's sequential rule applied to them in order -- the same alpha.
 static void line_search(Ctx& c, bool stage2, double& alpha, double& dlalpha) {
   Scope s(c.timers, "Lalpha_min");
-  double al[kBatchLS], L[kBatchLS], xm[kBatchLS];
-  al[0] = 0.0;
-  al[1] = 0.0 + kDx;
-  al[2] = 1.0;
+  double al[3] = {0.0, 0.0 + kDx, 1.0}, L[3], xm[3];
   eval_candidates(c, al, 3, stage2, L, xm);
-  const double L0 = L[0];
-  const double df = (L[1] - L0) / kDx;
-  dlalpha = df;
-  double lm = kHuge, alphamin = 0.0;
-  // Evaluated probes waiting to be consumed in order; alpha = 1 is ready.
-  double qa[kBatchLS] = {1.0}, qL[kBatchLS] = {L[2]}, qx[kBatchLS] = {xm[2]};
-  int qlen = 1, qpos = 0;
-  double next_a = 1.0 * 0.75;  // alpha of the probe after the queued ones
-  int next_batch = 2;  // probes per sweep after alpha = 1: 2, 4, 8, 8, ...
-  for (int i = 1; i <= kMaxLS; ++i) {
-    if (qpos == qlen) {
-      qlen = std::min(next_batch, kMaxLS - i + 1);
-      next_batch = std::min(kBatchLS, 2 * next_batch);
-      for (int k = 0; k < qlen; ++k) {
-        qa[k] = next_a;
-        next_a = next_a * 0.75;
+  LSState ls;
+  ls.L0 = L[0];
+  ls.df = (L[1] - ls.L0) / kDx;
+  dlalpha = ls.df;
+  ls.next_a = 1.0 * 0.75;
+  ls_take(c, ls, stage2, 1.0, L[2], xm[2]);
+  ls_continue_fp64(c, ls, stage2, 2);
+  alpha = ls.alphamin;
+}
+
+// Mixed path: the two FP64 slope probes (alpha = 0, dx) as in the
+// reference; the probes alpha = 1, 0.75, ... are screened with their
+// objective change relative to the alpha = 0 candidate X0,
+//   L(X_a) - L(X0) = sum F.dX (2 r0 + F.dX) + Lgam(X_a) - Lgam(X0),
+// dX = X_a - X0 (projected), products in FP32 and sums in FP64; the chosen
+// step then gets an FP64 objective and sufficient-decrease check, and if it
+// fails the reference's FP64 sequence continues from the next probe.
+static void line_search_mixed(Ctx& c, bool stage2, double& alpha, double& dlalpha) {
+  Scope s(c.timers, "Lalpha_min");
+  const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
+  const int64_t MN = (int64_t)M * N, DN = (int64_t)D * N;
+  double al[2] = {0.0, 0.0 + kDx}, L[2], xm[2];
+  eval_candidates(c, al, 2, stage2, L, xm);
+  const double Lgam0 = c.h.gam != 0 ? c.pin[kBatchLS + 0] : 0.0;
+  LSState ls;
+  ls.L0 = L[0];
+  ls.df = (L[1] - ls.L0) / kDx;
+  dlalpha = ls.df;
+  // keep the alpha = 0 candidate and its residual O - P (FP32)
+  CK(cudaMemcpyAsync(c.x0c.p, c.Xc.p, MN * sizeof(double), cudaMemcpyDeviceToDevice, c.st));
+  k_half_to32<<<elem_grid(DN), 256, 0, c.st>>>(c.Rst.p, DN, 1.0f, c.r0_32.p);
+  post_launch(c);
+  double qa[kBatchLS], xmin[kBatchLS], dres[kBatchLS], lg[kBatchLS];
+  const int g = elem_grid(MN), g2 = elem_grid(DN);
+  bool screened_stop = false;
+  double stop_a = 0.0;  // alpha of the probe where the screened sequence stopped
+  while (!ls.done && ls.i <= kMaxLS) {
+    const int nb = std::min(kBatchLS, kMaxLS - ls.i + 1);
+    for (int k = 0; k < nb; ++k) {
+      qa[k] = ls.next_a;
+      ls.next_a = ls.next_a * 0.75;
+    }
+    CK(cudaMemcpyAsync(c.alphas.p, qa, nb * sizeof(double), cudaMemcpyHostToDevice, c.st));
+    if (stage2) {
+      const int gb = cdiv(M, kRowThreads);
+      k_cand_proj2<<<dim3(gb, nb), kRowThreads, 0, c.st>>>(c.X.p, c.sn64.p, c.alphas.p, c.Xc.p, MN, c.maxr.p, M, N, 1,
+                                                            c.part2.p);
+      post_launch(c);
+      reduce_to(c, c.part2.p, gb, c.lsout.p + 2 * kBatchLS, nb, true, 0.0);
+    } else {
+      project_rows(c, c.X.p, c.sn64.p, c.alphas.p, c.Xc.p, nb);
+    }
+    if (c.h.gam != 0) {
+      const int gg = elem_grid((int64_t)(M - 1) * N);
+      k_gamma_part<<<dim3(gg, nb), 256, 0, c.st>>>(c.Xc.p, MN, M, N, c.h.gam, c.part2.p);
+      post_launch(c);
+      reduce_to(c, c.part2.p, gg, c.lsout.p + kBatchLS, nb);
+    }
+    k_delta32<<<dim3(g, nb), 256, 0, c.st>>>(c.Xc.p, c.x0c.p, MN, c.d32.p);
+    post_launch(c);
+    {
+      const int64_t want = 2 * 152;
+      const int R = D;
+      if ((int64_t)cdiv(R, 64) * cdiv(N, 64) * nb >= want)
+        k_band_gemm32<64, 64><<<dim3(cdiv(N, 64), cdiv(R, 64), nb), 256, 0, c.st>>>(
+            c.flo.p, c.fw.p, c.foff.p, c.fval32.p, c.d32.p, R, N, 1.0f, c.fdx32.p, nullptr, MN, DN);
+      else
+        k_band_gemm32<64, 32><<<dim3(cdiv(N, 32), cdiv(R, 64), nb), 128, 0, c.st>>>(
+            c.flo.p, c.fw.p, c.foff.p, c.fval32.p, c.d32.p, R, N, 1.0f, c.fdx32.p, nullptr, MN, DN);
+      post_launch(c);
+    }
+    k_dres_part<<<dim3(g2, nb), 256, 0, c.st>>>(c.fdx32.p, c.r0_32.p, c.flo.p, D, N, c.part.p);
+    post_launch(c);
+    reduce_to(c, c.part.p, g2, c.lsout.p + 3 * kBatchLS, nb);
+    CK(cudaMemcpyAsync(c.pin, c.lsout.p, 4 * kBatchLS * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    CK(cudaStreamSynchronize(c.st));
+    for (int k = 0; k < nb; ++k) {
+      xmin[k] = stage2 ? c.pin[2 * kBatchLS + k] : 0.0;
+      dres[k] = c.pin[3 * kBatchLS + k];
+      lg[k] = c.h.gam != 0 ? c.pin[kBatchLS + k] - Lgam0 : 0.0;
+    }
+    c.n_lsL += nb;
+    for (int k = 0; k < nb && !ls.done; ++k)
+      if (ls_take(c, ls, stage2, qa[k], ls.L0 + dres[k] + lg[k], xmin[k])) {
+        screened_stop = true;
+        stop_a = qa[k];
       }
-      eval_candidates(c, qa, qlen, stage2, qL, qx);
-      qpos = 0;
-    }
-    const double alpha_i = qa[qpos], Lp = qL[qpos], xmin = qx[qpos];
-    ++qpos;
-    const bool better = stage2 ? (Lp < lm && xmin >= -kFeasTol) : (Lp < lm);
-    if (better) {
-      lm = Lp;
-      alphamin = alpha_i;
-    }
-    if (c.verbose) {
-      ListLine l;
-      l.s("line search").i8(i).s("L=").r8(Lp).s("alpha=").r8(alpha_i).s("df(0)=").r8(df);
-      if (stage2) l.s("min(X)=").r8(xmin);
-      l.print();
-    }
-    const double armijo = std::fma(0.1 * alpha_i, df, L0);
-    const bool shrink = stage2 ? (Lp > armijo || xmin < -kFeasTol) : (Lp > armijo);
-    if (!shrink) break;
   }
-  alpha = alphamin;
+  // FP64 objective and sufficient-decrease check of the chosen step
+  if (ls.alphamin != 0.0) {
+    double a1[1] = {ls.alphamin}, Lv[1], xv[1];
+    eval_candidates(c, a1, 1, stage2, Lv, xv);
+    const double armijo = std::fma(0.1 * ls.alphamin, ls.df, ls.L0);
+    const bool ok = Lv[0] <= armijo && (!stage2 || xv[0] >= -kFeasTol);
+    if (!ok && screened_stop && ls.i <= kMaxLS) {
+      // continue the reference's sequence in FP64 after the screened stop
+      LSState f = ls;
+      f.done = false;
+      f.next_a = stop_a * 0.75;  // the probe after the screened stop
+      f.lm = (!stage2 || xv[0] >= -kFeasTol) ? Lv[0] : kHuge;
+      f.alphamin = (f.lm < kHuge) ? ls.alphamin : 0.0;
+      ls_continue_fp64(c, f, stage2, 2);
+      ls = f;
+    } else if (!ok && !(Lv[0] < ls.L0)) {
+      ls.alphamin = 0.0;  // no FP64 decrease: keep X (the reference's alpha = 0 case)
+    }
+  }
+  alpha = ls.alphamin;
 }
 
 // conv_test (1034-1067) on the context's X; leaves the full space selected.
@@ -952,7 +1077,8 @@ static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
     if (fp32) k_twometric<float><<<g, 256, 0, c.st>>>(c.cg32.sn.p, c.G.p, c.ik.p, mr, c.bdiag.p, bdfac, M, N, c.sn64.p);
     else k_twometric<double><<<g, 256, 0, c.st>>>(c.cg64.sn.p, c.G.p, c.ik.p, mr, c.bdiag.p, bdfac, M, N, c.sn64.p);
     post_launch(c);
-    line_search(c, !c.fullspace, st.alpha, st.dlalpha);
+    if (c.exact) line_search(c, !c.fullspace, st.alpha, st.dlalpha);
+    else line_search_mixed(c, !c.fullspace, st.alpha, st.dlalpha);
     // Mixed precision: once the FP32 Newton direction stops giving progress
     // the remaining iterations run the CG in FP64 (final refinement).
     if (c.precision == PQDTS_MIXED && !c.refine && !c.fullspace && (st.alpha == 0.0 || st.dlalpha >= 0.0))
