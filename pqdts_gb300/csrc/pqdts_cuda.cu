@@ -41,6 +41,7 @@ constexpr int kMaxCG = 50;                 // do j = 1, 50 (2036)
 constexpr int kMaxLS = 100;                // do i = 1, 100 (374, 420, 466)
 constexpr int kBatchLS = 8;                // step lengths evaluated per sweep
 constexpr int kElemGrid = 152 * 8;         // elementwise grids: 8 blocks per SM
+constexpr int kGR64 = 64, kGN64 = 64;      // FP32 product tile of the split-K transposed product
 
 struct Err : std::runtime_error {
   int code;
@@ -213,7 +214,10 @@ struct pqdts_ctx {
   // mixed-precision line search: alpha = 0 candidate, its residual (FP32),
   // candidate differences and their banded products (FP32)
   pqdts::DBuf<double> x0c;
-  pqdts::DBuf<float> r0_32, d32, fdx32;
+  pqdts::DBuf<float> r0_32, d32, fdx32, hpart32;
+  int hsplits = 1;  // K segments of the FP32 transposed product
+  pqdts::DBuf<double> Gf;  // mixed path: full-space gradient of X (version Gf_ver)
+  int64_t Gf_ver = -1;
   bool exact = true;  // FP64: every reduction in the oracle's order
   pqdts::DBuf<int> ipart;
   pqdts::DBuf<long long> icount;
@@ -227,7 +231,7 @@ struct pqdts_ctx {
   // version of X, bumped on every write; results keyed on it are reused
   int64_t xver = 0, R_ver = -1, G_ver = -1, L_ver = -1, rebuilt_ver = -1;
   bool G_full = true;
-  double L_cache = 0.0;
+  double L_cache = 0.0, Lgam_cache = 0.0;  // L of X (version L_ver) and its gamma term
   bool target_hit = false;
 };
 
@@ -309,6 +313,12 @@ static void setup_device(Ctx& c) {
     c.rsq32.alloc(M);
     c.cg32.alloc(MN, M, D * N);
     c.x0c.alloc(MN);
+    c.Gf.alloc(MN);
+    {
+      const int64_t ctas = (int64_t)cdiv(M, kGR64) * cdiv(N, kGN64);
+      c.hsplits = (int)std::min<int64_t>(8, std::max<int64_t>(1, (2 * 152 + ctas - 1) / ctas));
+      c.hpart32.alloc((size_t)c.hsplits * MN);
+    }
     c.r0_32.alloc(D * N);
     c.d32.alloc((size_t)kBatchLS * MN);
     c.fdx32.alloc((size_t)kBatchLS * D * N);
@@ -349,7 +359,7 @@ static void setup_device(Ctx& c) {
   // Initial X = 1/N (pqdts.f90:1834-1838) and maxr from the seeded stream.
   k_fill<<<elem_grid(MN), 256, 0, c.st>>>(MN, 1.0 / (double)N, c.X.p);
   post_launch(c);
-  c.R_ver = c.G_ver = c.L_ver = c.rebuilt_ver = -1;
+  c.R_ver = c.G_ver = c.L_ver = c.rebuilt_ver = c.Gf_ver = -1;
   touch_x(c);
   CK(cudaMemcpyAsync(c.maxr.p, c.h_maxr.data(), M * 4, cudaMemcpyHostToDevice, c.st));
   c.h2d += M * 4;
@@ -466,6 +476,7 @@ static double op_L(Ctx& c) {
   double L;
   fetch_objectives(c, 1, &L);
   c.L_cache = L;
+  c.Lgam_cache = (c.h.gam != 0 && !c.exact) ? c.pin[kBatchLS] : 0.0;
   c.L_ver = c.xver;
   return L;
 }
@@ -496,22 +507,22 @@ static TransShape trans_shape(int N) {
 
 template <typename T, bool HVP>
 static void launch_trans(Ctx& c, const T* tv, const T* R, const T* V, const T* rs, int reduced, T c2gam,
-                         const int8_t* ik, T* G, const T* W, double* dpart, const double* pred) {
+                         const int8_t* ik, T* G, const T* W, double* dpart, const double* pred, T* Gf = nullptr) {
   const int M = (int)c.h.M;
   const TransShape sh = trans_shape((int)c.h.N);
   DevBands bd = bands_of(c);
   switch (sh.C) {
     case 1:
-      k_trans<T, HVP, 1><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred);
+      k_trans<T, HVP, 1><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf);
       break;
     case 2:
-      k_trans<T, HVP, 2><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred);
+      k_trans<T, HVP, 2><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf);
       break;
     case 4:
-      k_trans<T, HVP, 4><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred);
+      k_trans<T, HVP, 4><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf);
       break;
     default:
-      k_trans<T, HVP, 8><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred);
+      k_trans<T, HVP, 8><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf);
       break;
   }
   post_launch(c);
@@ -521,11 +532,27 @@ static void launch_trans(Ctx& c, const T* tv, const T* R, const T* V, const T* r
 // space have not changed since they were computed (bitwise the same values).
 static void op_dL(Ctx& c) {
   Scope s(c.timers, "dL");
+  const int M = (int)c.h.M, N = (int)c.h.N;
   if (!c.fullspace) rebuild_x(c);
   if (c.G_ver == c.xver && c.G_full == c.fullspace) return;
-  ensure_R(c);
-  launch_trans<double, false>(c, c.tval.p, c.R.p, c.X.p, nullptr, c.fullspace ? 0 : 1, 2.0 * c.h.gam, nullptr, c.G.p,
-                              nullptr, nullptr, nullptr);
+  if (!c.exact && c.Gf_ver == c.xver) {
+    // mixed path: the full-space gradient of this X is known
+    if (c.fullspace) {
+      CK(cudaMemcpyAsync(c.G.p, c.Gf.p, (size_t)M * N * 8, cudaMemcpyDeviceToDevice, c.st));
+    } else {
+      k_reduced_from_full<<<M, std::min(256, std::max(32, cdiv(N, 32) * 32)), 0, c.st>>>(c.Gf.p, c.maxr.p, N, c.G.p);
+      post_launch(c);
+    }
+  } else {
+    ensure_R(c);
+    double* gf = (!c.exact && !c.fullspace) ? c.Gf.p : nullptr;
+    launch_trans<double, false>(c, c.tval.p, c.R.p, c.X.p, nullptr, c.fullspace ? 0 : 1, 2.0 * c.h.gam, nullptr,
+                                c.G.p, nullptr, nullptr, nullptr, gf);
+    if (!c.exact) {
+      if (c.fullspace) CK(cudaMemcpyAsync(c.Gf.p, c.G.p, (size_t)M * N * 8, cudaMemcpyDeviceToDevice, c.st));
+      c.Gf_ver = c.xver;
+    }
+  }
   c.G_ver = c.xver;
   c.G_full = c.fullspace;
 }
@@ -602,10 +629,16 @@ static void hvp32(Ctx& c, CGBufs<float>& b, const int8_t* ik, bool with_dot, con
   const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
   const float* src = c.fullspace ? b.p.p : b.V.p;
   band_gemm32(c, c.flo.p, c.fw.p, c.foff.p, c.fval32.p, src, D, N, 2.0f, b.R2.p, pred);
-  band_gemm32(c, c.tlo.p, c.tw.p, c.toff.p, c.tbval32.p, b.R2.p, M, N, 1.0f, b.Hp.p, pred);
+  // F^T.(2O): 64x64 tiles, the K range split so the grid fills the GPU;
+  // the epilogue sums the partial products in a fixed order
+  require(c.hpart32.p, "split-K partials");
+  k_band_gemm32<64, 64><<<dim3(cdiv(N, 64), cdiv(M, 64), c.hsplits), 256, 0, c.st>>>(
+      c.tlo.p, c.tw.p, c.toff.p, c.tbval32.p, b.R2.p, M, N, 1.0f, c.hpart32.p, pred, 0, (int64_t)M * N, c.hsplits);
+  post_launch(c);
   const int tb = std::min(256, std::max(32, cdiv(N, 32) * 32));
-  k_hvp_epi32<<<M, tb, 0, c.st>>>(b.Hp.p, b.p.p, c.fullspace ? nullptr : b.rs.p, c.maxr.p, c.fullspace ? 0 : 1,
-                                  (float)(2.0 * c.h.gam), ik, M, N, b.Hp.p, with_dot ? c.part.p : nullptr, pred);
+  k_hvp_epi32<<<M, tb, 0, c.st>>>(c.hpart32.p, b.p.p, c.fullspace ? nullptr : b.rs.p, c.maxr.p, c.fullspace ? 0 : 1,
+                                  (float)(2.0 * c.h.gam), ik, M, N, b.Hp.p, with_dot ? c.part.p : nullptr, pred,
+                                  c.hsplits);
   post_launch(c);
   if (with_dot) reduce_to(c, c.part.p, M, c.sc.p + SC_V2, 1, false, 0.0, pred);
 }
@@ -904,17 +937,20 @@ static void line_search_mixed(Ctx& c, bool stage2, double& alpha, double& dlalph
   Scope s(c.timers, "Lalpha_min");
   const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
   const int64_t MN = (int64_t)M * N, DN = (int64_t)D * N;
-  double al[2] = {0.0, 0.0 + kDx}, L[2], xm[2];
-  eval_candidates(c, al, 2, stage2, L, xm);
-  const double Lgam0 = c.h.gam != 0 ? c.pin[kBatchLS + 0] : 0.0;
-  LSState ls;
-  ls.L0 = L[0];
-  ls.df = (L[1] - ls.L0) / kDx;
-  dlalpha = ls.df;
-  // keep the alpha = 0 candidate and its residual O - P (FP32)
-  CK(cudaMemcpyAsync(c.x0c.p, c.Xc.p, MN * sizeof(double), cudaMemcpyDeviceToDevice, c.st));
-  k_half_to32<<<elem_grid(DN), 256, 0, c.st>>>(c.Rst.p, DN, 1.0f, c.r0_32.p);
+  // alpha = 0: the projection of the (feasible) iterate is the iterate to
+  // within ulps, so X, its objective and its residual R/2 serve as X0
+  const double L0 = op_L(c);
+  const double Lgam0 = c.Lgam_cache;
+  ensure_R(c);
+  CK(cudaMemcpyAsync(c.x0c.p, c.X.p, MN * sizeof(double), cudaMemcpyDeviceToDevice, c.st));
+  k_half_to32<<<elem_grid(DN), 256, 0, c.st>>>(c.R.p, DN, 0.5f, c.r0_32.p);
   post_launch(c);
+  double al[1] = {0.0 + kDx}, L[1], xm[1];
+  eval_candidates(c, al, 1, stage2, L, xm);
+  LSState ls;
+  ls.L0 = L0;
+  ls.df = (L[0] - ls.L0) / kDx;
+  dlalpha = ls.df;
   double qa[kBatchLS], xmin[kBatchLS], dres[kBatchLS], lg[kBatchLS];
   const int g = elem_grid(MN), g2 = elem_grid(DN);
   bool screened_stop = false;
@@ -1062,7 +1098,14 @@ static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
     if (!c.fullspace) {
       k_stage2_start<<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(c.X.p, c.maxr.p, M, N, 1);
       post_launch(c);
-      touch_x(c);
+      if (c.exact) {
+        touch_x(c);
+      } else {
+        // mixed path: the placeholder is replaced by the next rebuild, which
+        // restores X to within ulps; only the reduced gradient (new maxr)
+        // must be derived again
+        c.G_ver = -1;
+      }
     } else {
       set_full_space(c);
     }
