@@ -48,6 +48,21 @@ int pqdts_cuda_destroy(pqdts_ctx* ctx);
 int pqdts_cuda_last_error(pqdts_ctx* ctx, char* buf, int64_t len);
 /* Number of CUDA kernels this context has launched so far. */
 int pqdts_cuda_kernel_launches(pqdts_ctx* ctx, int64_t* count);
+/* Options of a context.  No counterpart in the reference (launch tuning of
+ * this implementation; results of the FP64 path do not depend on them).
+ *   "graphs"   1 (default): each chunk of CG iterations is replayed as one
+ *              captured CUDA graph; 0: the same kernels launched one by one.
+ *   "autotune" 1 (default): the banded products' launch schedule is timed on
+ *              the problem at set-up (once per size bucket per process);
+ *              0: heuristic shapes.  Takes effect at the next set_problem.
+ * Unknown names return PQDTS_E_ARG. */
+int pqdts_cuda_set_option(pqdts_ctx* ctx, const char* name, int64_t value);
+/* Reads an option above or a field of the schedule in use:
+ * "sched.fwd_tile", "sched.trn_tile" (0 = 64x64, 1 = 64x32, 2 = 32x32 FP32
+ * tiles of F.V and F^T.R), "sched.trn_splits" (K segments of F^T.R),
+ * "sched.trans_threads", "sched.trans_cols" (FP64 F^T product block shape),
+ * "sched.tuned" (1 = timed, 0 = heuristic), "graphs.captured" (graphs held). */
+int pqdts_cuda_get_option(pqdts_ctx* ctx, const char* name, int64_t* value);
 /* verbose = 1 prints the reference's stdout lines (iter, newton-pcg, line
  * search, positivity constraints) exactly as rank 0 of pqdts_omp.x. */
 int pqdts_cuda_set_verbose(pqdts_ctx* ctx, int32_t verbose);
@@ -166,13 +181,17 @@ int pqdts_cuda_timer(pqdts_ctx* ctx, const char* name, double* seconds, int64_t*
  * it replaces n_inst separate pqdts_omp.x runs).  Instance k uses
  * M[k], N[k], D[k], the bands band_lo/hi/vals + offsets, P + offset, gamma[k];
  * X holds sum_k M[k]*N[k] doubles (column-major per instance, in order),
- * starting points on entry and results on exit.  stats: PQDTS_NSTATS per
- * instance. */
+ * starting points on entry and results on exit.  target_L (may be null):
+ * per-instance objective targets as pqdts_cuda_set_objective_target.
+ * stats: PQDTS_NSTATS per instance.  Host workers (up to 8) each own a
+ * context and stream and take instances in order, so instances overlap on
+ * the device; each context's CG chunks replay as CUDA graphs and instances
+ * of one size bucket share one autotuned launch schedule. */
 int pqdts_cuda_solve_batch(int32_t device, int32_t n_inst, const int64_t* M, const int64_t* N, const int64_t* D,
                            const int64_t* band_lo, const int64_t* band_hi, const double* band_vals,
                            const int64_t* band_row_offset, const int64_t* band_val_offset, const double* P,
                            const int64_t* P_offset, const double* gamma, int32_t precision, int32_t mode,
-                           int32_t maxiiter, double conv_thres, double* X, double* stats);
+                           int32_t maxiiter, double conv_thres, const double* target_L, double* X, double* stats);
 
 #ifdef __cplusplus
 }

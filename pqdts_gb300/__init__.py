@@ -75,7 +75,9 @@ def lib():
         "pqdts_cuda_solve": [p, i32, i32, d, i32, i32, p, p, p],
         "pqdts_cuda_timer": [p, C.c_char_p, C.POINTER(d), C.POINTER(i64)],
         "pqdts_cuda_set_objective_target": [p, d],
-        "pqdts_cuda_solve_batch": [i32, i32, p, p, p, p, p, p, p, p, p, p, p, i32, i32, i32, d, p, p],
+        "pqdts_cuda_set_option": [p, C.c_char_p, i64],
+        "pqdts_cuda_get_option": [p, C.c_char_p, C.POINTER(i64)],
+        "pqdts_cuda_solve_batch": [i32, i32, p, p, p, p, p, p, p, p, p, p, p, i32, i32, i32, d, p, p, p],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -272,6 +274,21 @@ class Solver:
         """Extra stopping rule (off by default): stop once L <= target."""
         self._check(self._L.pqdts_cuda_set_objective_target(self.h, float(target)), "set_objective_target")
 
+    def set_option(self, name, value):
+        """"graphs" (CG chunks as CUDA graphs) or "autotune" (timed launch
+        schedules at set-up), 1 = on (default) / 0 = off."""
+        self._check(self._L.pqdts_cuda_set_option(self.h, name.encode(), int(value)), "set_option")
+
+    def get_option(self, name):
+        v = C.c_int64()
+        self._check(self._L.pqdts_cuda_get_option(self.h, name.encode(), C.byref(v)), "get_option")
+        return v.value
+
+    def schedule(self):
+        """Launch schedule of the banded products in use (autotuned or heuristic)."""
+        keys = ("fwd_tile", "trn_tile", "trn_splits", "trans_threads", "trans_cols", "tuned")
+        return {k: self.get_option("sched." + k) for k in keys}
+
     def kernel_launches(self):
         v = C.c_int64()
         self._check(self._L.pqdts_cuda_kernel_launches(self.h, C.byref(v)), "kernel_launches")
@@ -284,8 +301,9 @@ class Solver:
         return s.value, n.value
 
 
-def solve_batch(instances, X0=None, precision=FP64, mode=2, maxiter=100, eps=1e-6, device=0):
-    """Solve independent instances (uneven M, N, D, gamma) on one GPU."""
+def solve_batch(instances, X0=None, precision=FP64, mode=2, maxiter=100, eps=1e-6, device=0, targets=None):
+    """Solve independent instances (uneven M, N, D, gamma) on one GPU;
+    `targets`: optional per-instance objective targets (stop once L <= it)."""
     L = lib()
     k = len(instances)
     M = np.array([i.M for i in instances], np.int64)
@@ -304,9 +322,13 @@ def solve_batch(instances, X0=None, precision=FP64, mode=2, maxiter=100, eps=1e-
     else:
         X = np.concatenate([np.asfortranarray(x).ravel(order="F") for x in X0])
     stats = np.zeros(8 * k)
+    tg = None if targets is None else np.ascontiguousarray(targets, np.float64)
+    if tg is not None and tg.size != k:
+        raise ValueError("one target per instance")
     rc = L.pqdts_cuda_solve_batch(int(device), k, _ptr(M), _ptr(N), _ptr(D), _ptr(lo), _ptr(hi), _ptr(vals),
                                   _ptr(row_off), _ptr(val_off), _ptr(P), _ptr(P_off), _ptr(gam), int(precision),
-                                  int(mode), int(maxiter), float(eps), _ptr(X), _ptr(stats))
+                                  int(mode), int(maxiter), float(eps), None if tg is None else _ptr(tg), _ptr(X),
+                                  _ptr(stats))
     if rc != 0:
         raise PqdtsError(f"pqdts_cuda_solve_batch failed ({rc})")
     out, off = [], 0

@@ -10,12 +10,14 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <stdexcept>
@@ -41,7 +43,6 @@ constexpr int kMaxCG = 50;                 // do j = 1, 50 (2036)
 constexpr int kMaxLS = 100;                // do i = 1, 100 (374, 420, 466)
 constexpr int kBatchLS = 8;                // step lengths evaluated per sweep
 constexpr int kElemGrid = 152 * 8;         // elementwise grids: 8 blocks per SM
-constexpr int kGR64 = 64, kGN64 = 64;      // FP32 product tile of the split-K transposed product
 
 struct Err : std::runtime_error {
   int code;
@@ -57,10 +58,13 @@ struct Err : std::runtime_error {
                     std::to_string(__LINE__) + ")");                                                    \
   } while (0)
 
+// Device array that keeps its allocation when a later problem fits in it
+// (cudaFree synchronises the whole device: a context reused for a stream of
+// instances, as the batched solve does, allocates only when one grows).
 template <typename T>
 struct DBuf {
   T* p = nullptr;
-  size_t n = 0;
+  size_t n = 0, cap = 0;
   DBuf() = default;
   DBuf(const DBuf&) = delete;
   DBuf& operator=(const DBuf&) = delete;
@@ -68,13 +72,17 @@ struct DBuf {
   void release() {
     if (p) cudaFree(p);
     p = nullptr;
-    n = 0;
+    n = cap = 0;
   }
   void alloc(size_t count) {
-    release();
     if (count == 0) count = 1;
+    if (p && count <= cap) {
+      n = count;
+      return;
+    }
+    release();
     CK(cudaMalloc((void**)&p, count * sizeof(T)));
-    n = count;
+    n = cap = count;
   }
   void upload(const T* h, size_t count, cudaStream_t s, std::atomic<int64_t>* bytes) {
     alloc(count);
@@ -113,16 +121,57 @@ struct GpuTimers {
     CK(cudaEventCreate(&e));
     return e;
   }
+  // While a CUDA graph is being captured, spans become event-record nodes
+  // of that graph (events owned by the graph, harvested after each replay).
+  std::vector<Pending>* capture = nullptr;
+  std::vector<cudaEvent_t> capture_pool;  // created before the capture began
+  cudaEvent_t capture_ev() {
+    cudaEvent_t e = nullptr;
+    if (!capture_pool.empty()) {
+      e = capture_pool.back();
+      capture_pool.pop_back();
+    } else if (cudaEventCreate(&e) != cudaSuccess) {
+      e = nullptr;
+    }
+    return e;
+  }
   int begin(const char* n) {
+    if (capture) {
+      Pending p{id_of(n), capture_ev(), nullptr};
+      if (!p.a) throw Err(PQDTS_E_CUDA, "cudaEventCreate failed during graph capture");
+      capture->push_back(p);
+      CK(cudaEventRecordWithFlags(p.a, st, cudaEventRecordExternal));
+      return -(int)capture->size();
+    }
     Pending p{id_of(n), ev(), nullptr};
     CK(cudaEventRecord(p.a, st));
     pending.push_back(p);
     counts[p.id]++;
     return (int)pending.size() - 1;
   }
+  // Spans of a graph replay that has completed (the stream was synchronised).
+  void harvest(const std::vector<Pending>& spans) {
+    for (const auto& p : spans) {
+      float ms = 0;
+      if (p.b) CK(cudaEventElapsedTime(&ms, p.a, p.b));
+      secs[p.id] += ms * 1e-3;
+      counts[p.id]++;
+    }
+  }
   // Called from destructors: never throws; a failed record only loses the
   // sample (the CUDA error itself surfaces at the next checked call).
   void end(int tok) noexcept {
+    if (tok < 0) {
+      if (!capture) return;
+      Pending& p = (*capture)[-tok - 1];
+      p.b = capture_ev();
+      if (!p.b) return;
+      if (cudaEventRecordWithFlags(p.b, st, cudaEventRecordExternal) != cudaSuccess) {
+        cudaEventDestroy(p.b);
+        p.b = nullptr;
+      }
+      return;
+    }
     cudaEvent_t e = nullptr;
     if (!pool.empty()) {
       e = pool.back();
@@ -156,6 +205,7 @@ struct GpuTimers {
       if (p.b) cudaEventDestroy(p.b);
     }
     for (auto e : pool) cudaEventDestroy(e);
+    for (auto e : capture_pool) cudaEventDestroy(e);
   }
 };
 
@@ -164,6 +214,33 @@ struct Scope {
   int tok;
   Scope(GpuTimers& tt, const char* n) : t(tt), tok(tt.begin(n)) {}
   ~Scope() { t.end(tok); }
+};
+
+// One captured chunk of CG iterations, replayed with a single graph launch;
+// its kernel count and timer spans are credited per replay.
+struct CGGraph {
+  cudaGraphExec_t exec = nullptr;
+  std::vector<GpuTimers::Pending> spans;
+  int64_t kernels = 0;
+  void destroy() noexcept {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    for (auto& p : spans) {
+      if (p.a) cudaEventDestroy(p.a);
+      if (p.b) cudaEventDestroy(p.b);
+    }
+    spans.clear();
+  }
+};
+
+// Launch schedule of the banded products (autotuned per size bucket).
+struct Schedule {
+  int fwd_tile = 0;       // FP32 F.V tile: 0 = 64x64, 1 = 64x32, 2 = 32x32
+  int trn_tile = 0;       // FP32 F^T.R tile (same codes) ...
+  int trn_splits = 1;     // ... with its K range split in this many segments
+  int trans_threads = 0;  // FP64 F^T product: threads per row block (0 = heuristic)
+  int trans_cols = 0;     // ... and columns per thread
+  int tuned = 0;          // 1 = picked by timing, 0 = heuristic
 };
 
 // CG work vectors of one precision.
@@ -215,7 +292,6 @@ struct pqdts_ctx {
   // candidate differences and their banded products (FP32)
   pqdts::DBuf<double> x0c;
   pqdts::DBuf<float> r0_32, d32, fdx32, hpart32;
-  int hsplits = 1;  // K segments of the FP32 transposed product
   pqdts::DBuf<double> Gf;  // mixed path: full-space gradient of X (version Gf_ver)
   int64_t Gf_ver = -1;
   bool exact = true;  // FP64: every reduction in the oracle's order
@@ -233,6 +309,17 @@ struct pqdts_ctx {
   bool G_full = true;
   double L_cache = 0.0, Lgam_cache = 0.0;  // L of X (version L_ver) and its gamma term
   bool target_hit = false;
+  // CG chunks captured as CUDA graphs (keyed by variant; dropped whenever the
+  // device buffers are reallocated) and the products' launch schedule
+  std::map<std::array<uint64_t, 5>, pqdts::CGGraph> graphs;
+  bool use_graphs = true;
+  bool autotune = true;
+  pqdts::Schedule sched;
+  void drop_graphs() noexcept {
+    for (auto& kv : graphs) kv.second.destroy();
+    graphs.clear();
+  }
+  ~pqdts_ctx() { drop_graphs(); }
 };
 
 namespace pqdts {
@@ -290,6 +377,7 @@ static void read_back(Ctx& c, const double* dev, int count) {
 static void setup_device(Ctx& c) {
   HostProblem& h = c.h;
   const int64_t M = h.M, N = h.N, D = h.D, MN = M * N;
+  c.drop_graphs();  // their kernels hold the buffers about to be replaced
   c.flo.upload(h.flo.data(), D, c.st, &c.h2d);
   c.fw.upload(h.fw.data(), D, c.st, &c.h2d);
   c.foff.upload(h.foff.data(), D, c.st, &c.h2d);
@@ -314,11 +402,6 @@ static void setup_device(Ctx& c) {
     c.cg32.alloc(MN, M, D * N);
     c.x0c.alloc(MN);
     c.Gf.alloc(MN);
-    {
-      const int64_t ctas = (int64_t)cdiv(M, kGR64) * cdiv(N, kGN64);
-      c.hsplits = (int)std::min<int64_t>(8, std::max<int64_t>(1, (2 * 152 + ctas - 1) / ctas));
-      c.hpart32.alloc((size_t)c.hsplits * MN);
-    }
     c.r0_32.alloc(D * N);
     c.d32.alloc((size_t)kBatchLS * MN);
     c.fdx32.alloc((size_t)kBatchLS * D * N);
@@ -505,11 +588,13 @@ static TransShape trans_shape(int N) {
   return best;
 }
 
+// k_trans with an explicit block shape (every shape gives the same values:
+// each output accumulates its CSR row in ascending order in one thread).
 template <typename T, bool HVP>
-static void launch_trans(Ctx& c, const T* tv, const T* R, const T* V, const T* rs, int reduced, T c2gam,
-                         const int8_t* ik, T* G, const T* W, double* dpart, const double* pred, T* Gf = nullptr) {
+static void launch_trans_shape(Ctx& c, TransShape sh, const T* tv, const T* R, const T* V, const T* rs, int reduced,
+                               T c2gam, const int8_t* ik, T* G, const T* W, double* dpart, const double* pred,
+                               T* Gf = nullptr) {
   const int M = (int)c.h.M;
-  const TransShape sh = trans_shape((int)c.h.N);
   DevBands bd = bands_of(c);
   switch (sh.C) {
     case 1:
@@ -526,6 +611,15 @@ static void launch_trans(Ctx& c, const T* tv, const T* R, const T* V, const T* r
       break;
   }
   post_launch(c);
+}
+
+// k_trans with the context's schedule.
+template <typename T, bool HVP>
+static void launch_trans(Ctx& c, const T* tv, const T* R, const T* V, const T* rs, int reduced, T c2gam,
+                         const int8_t* ik, T* G, const T* W, double* dpart, const double* pred, T* Gf = nullptr) {
+  const TransShape sh = c.sched.trans_threads > 0 ? TransShape{c.sched.trans_threads, c.sched.trans_cols}
+                                                  : trans_shape((int)c.h.N);
+  launch_trans_shape<T, HVP>(c, sh, tv, R, V, rs, reduced, c2gam, ik, G, W, dpart, pred, Gf);
 }
 
 // dL(X) -> c.G (975-1032), reusing R and the gradient itself when X and the
@@ -604,23 +698,47 @@ static void hvp(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, const int8_t* ik
   if (with_dot) reduce_to(c, c.part.p, M, c.sc.p + SC_V2, 1, false, 0.0, pred);
 }
 
-// Mixed precision Hessian product Hp = H p in FP32 with the tiled band
-// products (F.V then F^T.(2O)) and the row epilogue; p.Hp -> sc[SC_V2].
-// Out (R x N) = scale * Band (R rows) . In, with the largest tile that
-// still gives at least two CTAs per SM (small problems need more, smaller
-// tiles to fill the GPU).
-static void band_gemm32(Ctx& c, const int32_t* lo, const int32_t* w, const int64_t* off, const float* vals,
-                        const float* In, int R, int N, float scale, float* Out, const double* pred) {
-  const int64_t want = 2 * 152;
-  auto ctas = [&](int tr, int tn) { return (int64_t)cdiv(R, tr) * cdiv(N, tn); };
-  if (ctas(64, 64) >= want) {
-    k_band_gemm32<64, 64><<<dim3(cdiv(N, 64), cdiv(R, 64)), 256, 0, c.st>>>(lo, w, off, vals, In, R, N, scale, Out, pred);
-  } else if (ctas(64, 32) >= want) {
-    k_band_gemm32<64, 32><<<dim3(cdiv(N, 32), cdiv(R, 64)), 128, 0, c.st>>>(lo, w, off, vals, In, R, N, scale, Out, pred);
-  } else {
-    k_band_gemm32<32, 32><<<dim3(cdiv(N, 32), cdiv(R, 32)), 64, 0, c.st>>>(lo, w, off, vals, In, R, N, scale, Out, pred);
+// Out (R x N) = scale * Band (R rows) . In with tile code `tile` (0 = 64x64,
+// 1 = 64x32, 2 = 32x32 rows x columns); grid.z = nz stacked products
+// (in_stride / out_stride apart) or, with splits > 1, the K segments of one
+// product (partials out_stride apart, summed by the consumer).
+static void launch_band_gemm32(Ctx& c, int tile, const int32_t* lo, const int32_t* w, const int64_t* off,
+                               const float* vals, const float* In, int R, int N, float scale, float* Out,
+                               const double* pred, int nz = 1, int64_t in_stride = 0, int64_t out_stride = 0,
+                               int splits = 1) {
+  switch (tile) {
+    case 0:
+      k_band_gemm32<64, 64><<<dim3(cdiv(N, 64), cdiv(R, 64), nz), 256, 0, c.st>>>(lo, w, off, vals, In, R, N, scale,
+                                                                                   Out, pred, in_stride, out_stride,
+                                                                                   splits);
+      break;
+    case 1:
+      k_band_gemm32<64, 32><<<dim3(cdiv(N, 32), cdiv(R, 64), nz), 128, 0, c.st>>>(lo, w, off, vals, In, R, N, scale,
+                                                                                   Out, pred, in_stride, out_stride,
+                                                                                   splits);
+      break;
+    default:
+      k_band_gemm32<32, 32><<<dim3(cdiv(N, 32), cdiv(R, 32), nz), 64, 0, c.st>>>(lo, w, off, vals, In, R, N, scale,
+                                                                                 Out, pred, in_stride, out_stride,
+                                                                                 splits);
+      break;
   }
   post_launch(c);
+}
+
+// CTAs of a tile code over an R x N output.
+static int64_t tile_ctas(int tile, int R, int N) {
+  const int tr = tile == 2 ? 32 : 64, tn = tile == 0 ? 64 : 32;
+  return (int64_t)cdiv(R, tr) * cdiv(N, tn);
+}
+
+// Heuristic tile: the largest that still gives two CTAs per SM (small
+// problems need more, smaller tiles to fill the GPU).
+static int heuristic_tile(int R, int N, int nz = 1) {
+  const int64_t want = 2 * 152;
+  if (tile_ctas(0, R, N) * nz >= want) return 0;
+  if (tile_ctas(1, R, N) * nz >= want) return 1;
+  return 2;
 }
 
 // Mixed precision Hessian product Hp = H p in FP32 with the tiled band
@@ -628,19 +746,91 @@ static void band_gemm32(Ctx& c, const int32_t* lo, const int32_t* w, const int64
 static void hvp32(Ctx& c, CGBufs<float>& b, const int8_t* ik, bool with_dot, const double* pred) {
   const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
   const float* src = c.fullspace ? b.p.p : b.V.p;
-  band_gemm32(c, c.flo.p, c.fw.p, c.foff.p, c.fval32.p, src, D, N, 2.0f, b.R2.p, pred);
-  // F^T.(2O): 64x64 tiles, the K range split so the grid fills the GPU;
-  // the epilogue sums the partial products in a fixed order
+  launch_band_gemm32(c, c.sched.fwd_tile, c.flo.p, c.fw.p, c.foff.p, c.fval32.p, src, D, N, 2.0f, b.R2.p, pred);
+  // F^T.(2O) with its K range split in trn_splits segments; the epilogue
+  // sums the partial products in a fixed order
   require(c.hpart32.p, "split-K partials");
-  k_band_gemm32<64, 64><<<dim3(cdiv(N, 64), cdiv(M, 64), c.hsplits), 256, 0, c.st>>>(
-      c.tlo.p, c.tw.p, c.toff.p, c.tbval32.p, b.R2.p, M, N, 1.0f, c.hpart32.p, pred, 0, (int64_t)M * N, c.hsplits);
-  post_launch(c);
+  const int parts = c.sched.trn_splits;
+  launch_band_gemm32(c, c.sched.trn_tile, c.tlo.p, c.tw.p, c.toff.p, c.tbval32.p, b.R2.p, M, N, 1.0f, c.hpart32.p,
+                     pred, parts, 0, (int64_t)M * N, parts);
   const int tb = std::min(256, std::max(32, cdiv(N, 32) * 32));
   k_hvp_epi32<<<M, tb, 0, c.st>>>(c.hpart32.p, b.p.p, c.fullspace ? nullptr : b.rs.p, c.maxr.p, c.fullspace ? 0 : 1,
                                   (float)(2.0 * c.h.gam), ik, M, N, b.Hp.p, with_dot ? c.part.p : nullptr, pred,
-                                  c.hsplits);
+                                  parts);
   post_launch(c);
   if (with_dot) reduce_to(c, c.part.p, M, c.sc.p + SC_V2, 1, false, 0.0, pred);
+}
+
+// A chunk of CG iterations captured as a CUDA graph (on first use of its
+// key: variant, space, constants; every kernel of it reads the context's
+// fixed buffers, so a replay is the same launches).
+template <class Body>
+static CGGraph& captured(Ctx& c, const std::array<uint64_t, 5>& key, int spans, Body&& body) {
+  auto it = c.graphs.find(key);
+  if (it != c.graphs.end()) return it->second;
+  CGGraph g;
+  for (int k = 0; k < 2 * spans; ++k) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    c.timers.capture_pool.push_back(e);
+  }
+  const int64_t l0 = c.launches;
+  cudaGraph_t graph = nullptr;
+  CK(cudaStreamBeginCapture(c.st, cudaStreamCaptureModeThreadLocal));
+  c.timers.capture = &g.spans;
+  try {
+    body();
+  } catch (...) {
+    c.timers.capture = nullptr;
+    cudaStreamEndCapture(c.st, &graph);
+    if (graph) cudaGraphDestroy(graph);
+    c.launches = l0;
+    g.destroy();
+    throw;
+  }
+  c.timers.capture = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(c.st, &graph);
+  g.kernels = c.launches - l0;
+  c.launches = l0;  // nothing ran yet: replays are counted
+  if (e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    g.destroy();
+    CK(e);
+  }
+  const cudaError_t e2 = cudaGraphInstantiate(&g.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e2 != cudaSuccess) {
+    g.destroy();
+    CK(e2);
+  }
+  return c.graphs.emplace(key, g).first->second;
+}
+
+// Queues CG iterations in chunks (4, then 8) and polls the exit flag after
+// each chunk; iterations queued after the exit are no-ops (each kernel reads
+// the flag first), the flag is also set at the iteration limit.  With graphs
+// on, a chunk is one replay of a captured graph.  Returns the iterations run.
+template <class Iter>
+static int cg_chunks(Ctx& c, std::array<uint64_t, 4> variant, Iter&& iteration) {
+  int queued = 0;
+  for (int chunk_no = 0;; ++chunk_no) {
+    const bool first = chunk_no == 0;
+    const int chunk = first ? 4 : 8;
+    if (c.use_graphs) {
+      CGGraph& gr = captured(c, {variant[0], variant[1], variant[2], variant[3], (uint64_t)first}, chunk, [&] {
+        for (int k = 0; k < chunk; ++k) iteration(first && k == 0);
+      });
+      CK(cudaGraphLaunch(gr.exec, c.st));
+      c.launches += gr.kernels;
+      queued += chunk;
+      read_back(c, c.sc.p, SC_NSC);
+      c.timers.harvest(gr.spans);
+    } else {
+      for (int k = 0; k < chunk && queued < kMaxCG; ++k, ++queued) iteration(queued == 0);
+      read_back(c, c.sc.p, SC_NSC);
+    }
+    if (c.pin[SC_DONE] != 0.0 || queued >= kMaxCG) return (int)c.pin[SC_ITER];
+  }
 }
 
 // The truncated-Newton PCG (2007-2090) in FP32 (mixed precision): the same
@@ -672,38 +862,30 @@ static void cg_solve32(Ctx& c, double bdfac) {
     l.s("positivity constraints").i8(nact).s("active of").i8(MN).r8((double)nact / (double)MN).print();
   }
   const int lift_blocks = cdiv((int64_t)M * 32, 256);
-  int queued = 0, chunk = 4, done_iters = 0;
-  for (;;) {
-    for (int k = 0; k < chunk && queued < kMaxCG; ++k, ++queued) {
-      if (c.fullspace) {
-        if (queued > 0) {
-          k_cg_pupdate<float><<<g, 256, 0, c.st>>>(c.sc.p, MN, b.p.p, b.z.p);
-          post_launch(c);
-        }
-      } else {
-        k_cg_lift32<<<lift_blocks, 256, 0, c.st>>>(queued > 0 ? c.sc.p : nullptr, queued > 0 ? 1 : 0, M, N, b.p.p,
-                                                   b.z.p, c.maxr.p, b.V.p, b.rs.p);
+  auto iteration = [&](bool first) {
+    if (c.fullspace) {
+      if (!first) {
+        k_cg_pupdate<float><<<g, 256, 0, c.st>>>(c.sc.p, MN, b.p.p, b.z.p);
         post_launch(c);
       }
-      {
-        Scope sb(c.timers, "BF");
-        hvp32(c, b, c.ik.p, true, c.sc.p);
-      }
-      k_cg_step32<<<g, 256, 0, c.st>>>(c.sc.p, c.rsq32.p, M, N, b.p.p, b.Hp.p, b.sn.p, b.r.p, b.z.p, c.part.p,
-                                       c.part2.p);
-      post_launch(c);
-      reduce_to(c, c.part.p, g, c.sc.p + SC_RZ, 1, false, 0.0, c.sc.p);
-      reduce_to(c, c.part2.p, g, c.sc.p + SC_RR, 1, false, 0.0, c.sc.p);
-      k_cg_scalars1<<<1, 1, 0, c.st>>>(c.sc.p, c.cglog.p, kMaxCG);
+    } else {
+      k_cg_lift32<<<lift_blocks, 256, 0, c.st>>>(first ? nullptr : c.sc.p, first ? 0 : 1, M, N, b.p.p, b.z.p,
+                                                 c.maxr.p, b.V.p, b.rs.p);
       post_launch(c);
     }
-    read_back(c, c.sc.p, SC_NSC);
-    if (c.pin[SC_DONE] != 0.0 || queued >= kMaxCG) {
-      done_iters = (int)c.pin[SC_ITER];
-      break;
+    {
+      Scope sb(c.timers, "BF");
+      hvp32(c, b, c.ik.p, true, c.sc.p);
     }
-    chunk = 8;
-  }
+    k_cg_step32<<<g, 256, 0, c.st>>>(c.sc.p, c.rsq32.p, M, N, b.p.p, b.Hp.p, b.sn.p, b.r.p, b.z.p, c.part.p,
+                                     c.part2.p);
+    post_launch(c);
+    reduce_to(c, c.part.p, g, c.sc.p + SC_RZ, 1, false, 0.0, c.sc.p);
+    reduce_to(c, c.part2.p, g, c.sc.p + SC_RR, 1, false, 0.0, c.sc.p);
+    k_cg_scalars1<<<1, 1, 0, c.st>>>(c.sc.p, c.cglog.p, kMaxCG);
+    post_launch(c);
+  };
+  const int done_iters = cg_chunks(c, {0, (uint64_t)c.fullspace, 0, 0}, iteration);
   c.n_cg += done_iters;
   if (c.verbose) {
     std::vector<double> lg(4 * kMaxCG);
@@ -756,53 +938,46 @@ static void cg_solve(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, double bdfa
     ListLine l;
     l.s("positivity constraints").i8(nact).s("active of").i8(MN).r8((double)nact / (double)MN).print();
   }
-  int done_iters = 0;
-  int queued = 0;
-  int chunk = 4;
-  for (;;) {
-    for (int k = 0; k < chunk && queued < kMaxCG; ++k, ++queued) {
-      if (queued > 0) {
-        if (c.fullspace) {
-          k_cg_pupdate<T><<<g, 256, 0, c.st>>>(c.sc.p, MN, b.p.p, b.z.p);
-          post_launch(c);
-        } else {
-          k_cg_lift<T><<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(c.sc.p, 1, M, N, b.p.p, b.z.p, c.maxr.p,
-                                                                         b.V.p, b.rs.p);
-          post_launch(c);
-        }
-      } else if (!c.fullspace) {
-        k_cg_lift<T><<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(nullptr, 0, M, N, b.p.p, b.z.p, c.maxr.p, b.V.p,
+  auto iteration = [&](bool first) {
+    if (!first) {
+      if (c.fullspace) {
+        k_cg_pupdate<T><<<g, 256, 0, c.st>>>(c.sc.p, MN, b.p.p, b.z.p);
+        post_launch(c);
+      } else {
+        k_cg_lift<T><<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(c.sc.p, 1, M, N, b.p.p, b.z.p, c.maxr.p, b.V.p,
                                                                        b.rs.p);
         post_launch(c);
       }
-      {
-        Scope sb(c.timers, "BF");
-        hvp<T>(c, b, fv, tv, c.ik.p, !exact, c.sc.p);
-      }
-      if constexpr (kF64)
-        if (exact) dot_dev(c, b.p.p, b.Hp.p, c.sc.p + SC_V2, c.sc.p);
-      k_cg_step<T><<<g, 256, 0, c.st>>>(c.sc.p, c.bdiag.p, bdfac, M, N, b.p.p, b.Hp.p, b.sn.p, b.r.p, b.z.p, c.part.p,
-                                        c.part2.p);
-      post_launch(c);
-      if (exact) {
-        if constexpr (kF64) {
-          static_assert(SC_RR - SC_RZ == 1, "scalar layout");
-          dot2_exact(c, b.r.p, b.z.p, c.sc.p + SC_RZ, 1, c.sc.p);
-        }
-      } else {
-        reduce_to(c, c.part.p, g, c.sc.p + SC_RZ, 1, false, 0.0, c.sc.p);
-        reduce_to(c, c.part2.p, g, c.sc.p + SC_RR, 1, false, 0.0, c.sc.p);
-      }
-      k_cg_scalars1<<<1, 1, 0, c.st>>>(c.sc.p, c.cglog.p, kMaxCG);
+    } else if (!c.fullspace) {
+      k_cg_lift<T><<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(nullptr, 0, M, N, b.p.p, b.z.p, c.maxr.p, b.V.p,
+                                                                     b.rs.p);
       post_launch(c);
     }
-    read_back(c, c.sc.p, SC_NSC);
-    if (c.pin[SC_DONE] != 0.0 || queued >= kMaxCG) {
-      done_iters = (int)c.pin[SC_ITER];
-      break;
+    {
+      Scope sb(c.timers, "BF");
+      hvp<T>(c, b, fv, tv, c.ik.p, !exact, c.sc.p);
     }
-    chunk = 8;
-  }
+    if constexpr (kF64)
+      if (exact) dot_dev(c, b.p.p, b.Hp.p, c.sc.p + SC_V2, c.sc.p);
+    k_cg_step<T><<<g, 256, 0, c.st>>>(c.sc.p, c.bdiag.p, bdfac, M, N, b.p.p, b.Hp.p, b.sn.p, b.r.p, b.z.p, c.part.p,
+                                      c.part2.p);
+    post_launch(c);
+    if (exact) {
+      if constexpr (kF64) {
+        static_assert(SC_RR - SC_RZ == 1, "scalar layout");
+        dot2_exact(c, b.r.p, b.z.p, c.sc.p + SC_RZ, 1, c.sc.p);
+      }
+    } else {
+      reduce_to(c, c.part.p, g, c.sc.p + SC_RZ, 1, false, 0.0, c.sc.p);
+      reduce_to(c, c.part2.p, g, c.sc.p + SC_RR, 1, false, 0.0, c.sc.p);
+    }
+    k_cg_scalars1<<<1, 1, 0, c.st>>>(c.sc.p, c.cglog.p, kMaxCG);
+    post_launch(c);
+  };
+  uint64_t bdbits;
+  std::memcpy(&bdbits, &bdfac, 8);
+  const uint64_t kind = kF64 ? (exact ? 1 : 2) : 3;
+  const int done_iters = cg_chunks(c, {kind, (uint64_t)c.fullspace, bdbits, 0}, iteration);
   c.n_cg += done_iters;
   if (c.verbose) {
     std::vector<double> lg(4 * kMaxCG);
@@ -979,17 +1154,8 @@ static void line_search_mixed(Ctx& c, bool stage2, double& alpha, double& dlalph
     }
     k_delta32<<<dim3(g, nb), 256, 0, c.st>>>(c.Xc.p, c.x0c.p, MN, c.d32.p);
     post_launch(c);
-    {
-      const int64_t want = 2 * 152;
-      const int R = D;
-      if ((int64_t)cdiv(R, 64) * cdiv(N, 64) * nb >= want)
-        k_band_gemm32<64, 64><<<dim3(cdiv(N, 64), cdiv(R, 64), nb), 256, 0, c.st>>>(
-            c.flo.p, c.fw.p, c.foff.p, c.fval32.p, c.d32.p, R, N, 1.0f, c.fdx32.p, nullptr, MN, DN);
-      else
-        k_band_gemm32<64, 32><<<dim3(cdiv(N, 32), cdiv(R, 64), nb), 128, 0, c.st>>>(
-            c.flo.p, c.fw.p, c.foff.p, c.fval32.p, c.d32.p, R, N, 1.0f, c.fdx32.p, nullptr, MN, DN);
-      post_launch(c);
-    }
+    launch_band_gemm32(c, heuristic_tile(D, N, nb), c.flo.p, c.fw.p, c.foff.p, c.fval32.p, c.d32.p, D, N, 1.0f,
+                       c.fdx32.p, nullptr, nb, MN, DN);
     k_dres_part<<<dim3(g2, nb), 256, 0, c.st>>>(c.fdx32.p, c.r0_32.p, c.flo.p, D, N, c.part.p);
     post_launch(c);
     reduce_to(c, c.part.p, g2, c.lsout.p + 3 * kBatchLS, nb);
@@ -1274,6 +1440,169 @@ static void solve(Ctx& c, int mode, int maxiiter, double conv_thres, int start_s
   fill_stats(c, st, wall() - t0, stats);
 }
 
+// ---------------------------------------------------------------------------
+// Autotuner: the banded products' launch schedule (FP32 tile shapes and K
+// splits, FP64 transposed-product block shape) timed on this problem's F at
+// set-up and remembered for the process per size bucket (device, precision,
+// N, and the log2 buckets of M, D and the mean band width), so instances of
+// one bucket (a resampled or gamma-swept batch) are tuned once.
+// ---------------------------------------------------------------------------
+static std::mutex g_sched_mu;
+static std::map<std::array<int64_t, 6>, Schedule> g_sched;
+
+static int ilog2_ceil(int64_t v) {
+  int k = 0;
+  while (((int64_t)1 << k) < v) ++k;
+  return k;
+}
+
+struct EventPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+  EventPair() {
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+  }
+  ~EventPair() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+};
+
+// Mean device time of one call of fn (ms): one untimed call, then `reps`.
+template <class F>
+static float time_calls(Ctx& c, int reps, F&& fn) {
+  fn();
+  EventPair ev;
+  CK(cudaEventRecord(ev.a, c.st));
+  for (int r = 0; r < reps; ++r) fn();
+  CK(cudaEventRecord(ev.b, c.st));
+  CK(cudaEventSynchronize(ev.b));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, ev.a, ev.b));
+  return ms / (float)reps;
+}
+
+// A schedule is only timed when one launch of the heuristic is shorter than
+// this (large problems fill the GPU with the heuristic's shapes anyway).
+constexpr float kTuneMaxMs = 20.0f;
+constexpr int kTuneReps = 3;
+
+static Schedule heuristic_schedule(const HostProblem& h) {
+  Schedule s;
+  const int M = (int)h.M, N = (int)h.N, D = (int)h.D;
+  s.fwd_tile = heuristic_tile(D, N);
+  s.trn_tile = 0;
+  const int64_t ctas = tile_ctas(0, M, N);
+  s.trn_splits = (int)std::min<int64_t>(8, std::max<int64_t>(1, (2 * 152 + ctas - 1) / ctas));
+  const TransShape sh = trans_shape(N);
+  s.trans_threads = sh.threads;
+  s.trans_cols = sh.C;
+  return s;
+}
+
+static void tune_schedule(Ctx& c, Schedule& s) {
+  const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
+  const int64_t MN = (int64_t)M * N;
+  // FP64 transposed product: for each column count C, the thread count with
+  // the fewest passes over the CSR row, then the fewest idle lanes
+  {
+    CGBufs<double>& b = c.cg64;
+    CK(cudaMemsetAsync(b.R2.p, 0, b.R2.n * sizeof(double), c.st));
+    CK(cudaMemsetAsync(b.p.p, 0, b.p.n * sizeof(double), c.st));
+    auto run = [&](TransShape sh) {
+      launch_trans_shape<double, true>(c, sh, c.tval.p, b.R2.p, b.p.p, nullptr, 0, 2.0 * c.h.gam, nullptr, b.Hp.p,
+                                       nullptr, nullptr, nullptr);
+    };
+    const TransShape h0{s.trans_threads, s.trans_cols};
+    float best = time_calls(c, kTuneReps, [&] { run(h0); });
+    if (best < kTuneMaxMs) {
+      for (int C : {1, 2, 4, 8}) {
+        TransShape cand{0, C};
+        int64_t bp = INT64_MAX, bw = INT64_MAX;
+        for (int t = 32; t <= 256; t += 32) {
+          const int64_t per = (int64_t)t * C, passes = (N + per - 1) / per, waste = passes * per - N;
+          if (passes < bp || (passes == bp && waste < bw)) {
+            bp = passes;
+            bw = waste;
+            cand.threads = t;
+          }
+        }
+        if (cand.threads == h0.threads && cand.C == h0.C) continue;
+        const float t = time_calls(c, kTuneReps, [&] { run(cand); });
+        if (t < best) {
+          best = t;
+          s.trans_threads = cand.threads;
+          s.trans_cols = cand.C;
+        }
+      }
+    }
+  }
+  if (c.precision != PQDTS_MIXED) return;
+  CGBufs<float>& b = c.cg32;
+  CK(cudaMemsetAsync(b.p.p, 0, b.p.n * sizeof(float), c.st));
+  CK(cudaMemsetAsync(b.R2.p, 0, b.R2.n * sizeof(float), c.st));
+  auto fwd = [&](int tile) {
+    launch_band_gemm32(c, tile, c.flo.p, c.fw.p, c.foff.p, c.fval32.p, b.p.p, D, N, 2.0f, b.R2.p, nullptr);
+  };
+  float best = time_calls(c, kTuneReps, [&] { fwd(s.fwd_tile); });
+  if (best < kTuneMaxMs)
+    for (int tile = 0; tile < 3; ++tile) {
+      if (tile == s.fwd_tile) continue;
+      const float t = time_calls(c, kTuneReps, [&] { fwd(tile); });
+      if (t < best) {
+        best = t;
+        s.fwd_tile = tile;
+      }
+    }
+  // transposed product: tile x K splits, partials of at most 1 GiB
+  const int max_splits = (int)std::max<int64_t>(1, std::min<int64_t>(8, ((int64_t)1 << 30) / (MN * 4)));
+  c.hpart32.alloc((size_t)std::max(max_splits, s.trn_splits) * MN);
+  auto trn = [&](int tile, int sp) {
+    launch_band_gemm32(c, tile, c.tlo.p, c.tw.p, c.toff.p, c.tbval32.p, b.R2.p, M, N, 1.0f, c.hpart32.p, nullptr,
+                       sp, 0, MN, sp);
+  };
+  best = time_calls(c, kTuneReps, [&] { trn(s.trn_tile, s.trn_splits); });
+  if (best < kTuneMaxMs)
+    for (int tile = 0; tile < 3; ++tile)
+      for (int sp : {1, 2, 3, 4, 6, 8}) {
+        if (sp > max_splits || (tile == s.trn_tile && sp == s.trn_splits)) continue;
+        if (tile_ctas(tile, M, N) * sp > 16 * 152) continue;
+        const float t = time_calls(c, kTuneReps, [&] { trn(tile, sp); });
+        // more partials cost the epilogue a read each: require a clear gain
+        if (t < best * (sp > s.trn_splits ? 0.97f : 1.0f)) {
+          best = t;
+          s.trn_tile = tile;
+          s.trn_splits = sp;
+        }
+      }
+}
+
+static void choose_schedule(Ctx& c) {
+  const HostProblem& h = c.h;
+  Schedule s = heuristic_schedule(h);
+  if (c.autotune) {
+    const int64_t wavg = h.D > 0 ? std::max<int64_t>(1, h.nnz() / h.D) : 1;
+    const std::array<int64_t, 6> key{c.device, c.precision, h.N, ilog2_ceil(h.M), ilog2_ceil(h.D), ilog2_ceil(wavg)};
+    std::lock_guard<std::mutex> lk(g_sched_mu);
+    auto it = g_sched.find(key);
+    if (it != g_sched.end()) {
+      s = it->second;
+    } else {
+      tune_schedule(c, s);
+      s.tuned = 1;
+      g_sched[key] = s;
+    }
+  }
+  c.sched = s;
+  if (c.precision == PQDTS_MIXED) {
+    const size_t need = (size_t)s.trn_splits * (size_t)h.M * (size_t)h.N;
+    if (c.hpart32.n != need) c.hpart32.alloc(need);
+  } else {
+    c.hpart32.release();
+  }
+  CK(cudaStreamSynchronize(c.st));
+}
+
 // Problem set-up shared by the entry points.
 static void init_problem(Ctx& c, HostProblem&& h, int precision, SeededStream& rng) {
   if (precision != PQDTS_FP64 && precision != PQDTS_MIXED) throw Err(PQDTS_E_ARG, "precision must be 0 or 1");
@@ -1283,6 +1612,7 @@ static void init_problem(Ctx& c, HostProblem&& h, int precision, SeededStream& r
   c.h_maxr = initial_maxr(c.h.M, c.h.N, rng);
   c.precision = precision;
   setup_device(c);
+  choose_schedule(c);
 }
 
 static void check_sizes(int64_t M, int64_t N, int64_t D) {
@@ -1703,6 +2033,38 @@ int pqdts_cuda_set_objective_target(pqdts_ctx* c, double target) {
   return PQDTS_OK;
 }
 
+int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
+  return guarded(c, [&] {
+    if (!name) throw pqdts::Err(PQDTS_E_ARG, "option name is null");
+    const std::string n = name;
+    if (n == "graphs") {
+      c->use_graphs = value != 0;
+    } else if (n == "autotune") {
+      c->autotune = value != 0;
+    } else {
+      throw pqdts::Err(PQDTS_E_ARG, "unknown option " + n);
+    }
+  });
+}
+
+int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
+  return guarded(c, [&] {
+    if (!name || !value) throw pqdts::Err(PQDTS_E_ARG, "null argument");
+    const std::string n = name;
+    const pqdts::Schedule& s = c->sched;
+    if (n == "graphs") *value = c->use_graphs;
+    else if (n == "autotune") *value = c->autotune;
+    else if (n == "sched.fwd_tile") *value = s.fwd_tile;
+    else if (n == "sched.trn_tile") *value = s.trn_tile;
+    else if (n == "sched.trn_splits") *value = s.trn_splits;
+    else if (n == "sched.trans_threads") *value = s.trans_threads;
+    else if (n == "sched.trans_cols") *value = s.trans_cols;
+    else if (n == "sched.tuned") *value = s.tuned;
+    else if (n == "graphs.captured") *value = (int64_t)c->graphs.size();
+    else throw pqdts::Err(PQDTS_E_ARG, "unknown option " + n);
+  });
+}
+
 int pqdts_cuda_timer(pqdts_ctx* c, const char* name, double* seconds, int64_t* count) {
   return guarded(c, [&] {
     c->timers.flush();
@@ -1721,7 +2083,8 @@ int pqdts_cuda_solve_batch(int32_t device, int32_t n_inst, const int64_t* M, con
                            const int64_t* band_lo, const int64_t* band_hi, const double* band_vals,
                            const int64_t* band_row_offset, const int64_t* band_val_offset, const double* P,
                            const int64_t* P_offset, const double* gamma, int32_t precision, int32_t mode,
-                           int32_t maxiiter, double conv_thres, double* X, double* stats) {
+                           int32_t maxiiter, double conv_thres, const double* target_L, double* X,
+                           double* stats) {
   if (n_inst <= 0 || !M || !N || !D || !band_lo || !band_hi || !band_vals || !band_row_offset || !band_val_offset ||
       !P || !P_offset || !gamma || !X)
     return PQDTS_E_ARG;
@@ -1748,6 +2111,7 @@ int pqdts_cuda_solve_batch(int32_t device, int32_t n_inst, const int64_t* M, con
       r = pqdts_cuda_set_problem(c, M[k], N[k], D[k], lo, hi, band_vals + band_val_offset[k], P + P_offset[k],
                                  gamma[k], precision);
       if (r == PQDTS_OK) r = pqdts_cuda_set_x(c, X + xoff[k]);
+      if (r == PQDTS_OK) r = pqdts_cuda_set_objective_target(c, target_L ? target_L[k] : 0.0);
       if (r == PQDTS_OK)
         r = pqdts_cuda_solve(c, mode, maxiiter, conv_thres, 1, 0, nullptr, nullptr,
                              stats ? stats + (int64_t)k * PQDTS_NSTATS : nullptr);

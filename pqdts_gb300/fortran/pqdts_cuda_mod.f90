@@ -32,6 +32,21 @@ module pqdts_cuda_mod
       integer(c_int64_t), value :: len
     end function
 
+    ! name: "graphs" or "autotune" (NUL-terminated, e.g. "graphs"//c_null_char)
+    integer(c_int32_t) function pqdts_cuda_set_option(ctx, name, value) bind(C, name="pqdts_cuda_set_option")
+      import :: c_int32_t, c_int64_t, c_ptr, c_char
+      type(c_ptr), value :: ctx
+      character(kind=c_char) :: name(*)
+      integer(c_int64_t), value :: value
+    end function
+
+    integer(c_int32_t) function pqdts_cuda_get_option(ctx, name, value) bind(C, name="pqdts_cuda_get_option")
+      import :: c_int32_t, c_int64_t, c_ptr, c_char
+      type(c_ptr), value :: ctx
+      character(kind=c_char) :: name(*)
+      integer(c_int64_t) :: value
+    end function
+
     integer(c_int32_t) function pqdts_cuda_set_verbose(ctx, verbose) bind(C, name="pqdts_cuda_set_verbose")
       import :: c_int32_t, c_ptr
       type(c_ptr), value :: ctx
@@ -103,6 +118,13 @@ module pqdts_cuda_mod
       real(c_double) :: V(*), HV(*)
     end function
 
+    ! BF in the mixed-precision solver's FP32 arithmetic (PQDTS_MIXED problems)
+    integer(c_int32_t) function pqdts_cuda_BF32(ctx, V, HV) bind(C, name="pqdts_cuda_BF32")
+      import :: c_int32_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      real(c_double) :: V(*), HV(*)
+    end function
+
     ! subroutine Bdiag(BD), pqdts.f90:208
     integer(c_int32_t) function pqdts_cuda_Bdiag(ctx, BD) bind(C, name="pqdts_cuda_Bdiag")
       import :: c_int32_t, c_double, c_ptr
@@ -158,6 +180,84 @@ module pqdts_cuda_mod
       type(c_funptr), value :: stage_cb
       type(c_ptr), value :: user
       real(c_double) :: stats(8)
+    end function
+
+    integer(c_int32_t) function pqdts_cuda_kernel_launches(ctx, count) bind(C, name="pqdts_cuda_kernel_launches")
+      import :: c_int32_t, c_int64_t, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int64_t) :: count
+    end function
+
+    integer(c_int32_t) function pqdts_cuda_get_bands(ctx, band_lo, band_hi, nnz) bind(C, name="pqdts_cuda_get_bands")
+      import :: c_int32_t, c_int64_t, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int64_t) :: band_lo(*), band_hi(*), nnz
+    end function
+
+    integer(c_int32_t) function pqdts_cuda_init_x(ctx) bind(C, name="pqdts_cuda_init_x")
+      import :: c_int32_t, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+
+    integer(c_int32_t) function pqdts_cuda_get_stream(ctx, stream) bind(C, name="pqdts_cuda_get_stream")
+      import :: c_int32_t, c_ptr
+      type(c_ptr), value :: ctx
+      type(c_ptr) :: stream
+    end function
+
+    integer(c_int32_t) function pqdts_cuda_transfer_bytes(ctx, h2d, d2h) bind(C, name="pqdts_cuda_transfer_bytes")
+      import :: c_int32_t, c_int64_t, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int64_t) :: h2d, d2h
+    end function
+
+    integer(c_int32_t) function pqdts_cuda_get_maxr(ctx, maxr) bind(C, name="pqdts_cuda_get_maxr")
+      import :: c_int32_t, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int32_t) :: maxr(*)
+    end function
+
+    ! redO local part, pqdts.f90:707-736: O(N,D) column-major
+    integer(c_int32_t) function pqdts_cuda_redO(ctx, O) bind(C, name="pqdts_cuda_redO")
+      import :: c_int32_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      real(c_double) :: O(*)
+    end function
+
+    ! device pointers d_y, d_x and a cudaStream_t (no counterpart in the reference)
+    integer(c_int32_t) function pqdts_cuda_simplexproj_noalloc(d_y, d_x, len, rows, stream) &
+        bind(C, name="pqdts_cuda_simplexproj_noalloc")
+      import :: c_int32_t, c_int64_t, c_ptr
+      type(c_ptr), value :: d_y, d_x, stream
+      integer(c_int64_t), value :: len, rows
+    end function
+
+    integer(c_int32_t) function pqdts_cuda_set_objective_target(ctx, target) &
+        bind(C, name="pqdts_cuda_set_objective_target")
+      import :: c_int32_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      real(c_double), value :: target
+    end function
+
+    integer(c_int32_t) function pqdts_cuda_timer(ctx, name, seconds, count) bind(C, name="pqdts_cuda_timer")
+      import :: c_int32_t, c_int64_t, c_double, c_ptr, c_char
+      type(c_ptr), value :: ctx
+      character(kind=c_char) :: name(*)
+      real(c_double) :: seconds
+      integer(c_int64_t) :: count
+    end function
+
+    ! target_L: pass c_null_ptr or c_loc of n_inst targets
+    integer(c_int32_t) function pqdts_cuda_solve_batch(device, n_inst, M, N, D, band_lo, band_hi, band_vals, &
+                                                       band_row_offset, band_val_offset, P, P_offset, gamma, &
+                                                       precision, mode, maxiiter, conv_thres, target_L, X, stats) &
+        bind(C, name="pqdts_cuda_solve_batch")
+      import :: c_int32_t, c_int64_t, c_double, c_ptr
+      integer(c_int32_t), value :: device, n_inst, precision, mode, maxiiter
+      integer(c_int64_t) :: M(*), N(*), D(*), band_lo(*), band_hi(*), band_row_offset(*), band_val_offset(*), P_offset(*)
+      real(c_double) :: band_vals(*), P(*), gamma(*), X(*), stats(*)
+      real(c_double), value :: conv_thres
+      type(c_ptr), value :: target_L
     end function
   end interface
 end module pqdts_cuda_mod

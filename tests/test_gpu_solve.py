@@ -97,6 +97,14 @@ def test_batch_matches_single(built):
     for inst, X, st in zip(insts, Xs, stats):
         Xs1, s1, _ = _solve_gpu(inst, maxiter=100)
         assert st["L"] == s1["L"] and np.array_equal(X, Xs1)
+    # mixed batch to per-instance objective targets (the batched benchmark's
+    # stopping rule): each ends at or below its target, feasible
+    L64 = np.array([st["L"] for st in stats])
+    tg = L64 * (1.0 + 1e-6)
+    Xm, sm = pq.solve_batch(insts, precision=pq.MIXED, maxiter=400, eps=1e-300, targets=tg)
+    for X, st, t in zip(Xm, sm, tg):
+        assert st["L"] <= t
+        _feasible(X)
 
 
 @pytest.mark.parametrize("which", ["cfg1", "small"])
@@ -110,3 +118,44 @@ def test_fp64_tight_tolerance_matches_oracle(built, request, which):
     assert abs(st["L"] - so["L"]) <= OBJ_REL * abs(so["L"])
     assert np.max(np.abs(X - Xo)) <= PI_ABS
     _feasible(X)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_graphs_and_autotune_do_not_change_results(built, small, precision):
+    """CG chunks replayed as CUDA graphs and autotuned launch shapes give the
+    same bits as one-by-one launches with heuristic shapes (same kernels in
+    the same order; every product's summation order is shape independent)."""
+    import pqdts_gb300 as pq
+
+    out = []
+    # mixed: the FP32 split-K partial count is part of the schedule and
+    # changes roundings, so both runs use the heuristic shapes
+    tuned = 1 if precision == 0 else 0
+    for graphs, tune in ((1, tuned), (0, 0)):
+        with pq.Solver(0) as s:
+            s.set_option("graphs", graphs)
+            s.set_option("autotune", tune)
+            s.set_instance(small, precision)
+            st = s.solve(mode=2, maxiter=200, eps=small.eps)
+            sched = s.schedule()
+            captured = s.get_option("graphs.captured")
+            bf = s.timer("BF")
+            out.append((s.get_x(), st, sched, captured, bf))
+    (X1, s1, sch1, cap1, bf1), (X0, s0, sch0, cap0, bf0) = out
+    assert cap1 > 0 and cap0 == 0
+    assert sch0["tuned"] == 0
+    assert bf1[1] >= s1["cg"] and bf1[0] > 0  # Hessian products timed inside the graphs
+    assert sch1["tuned"] == tuned and sch1["trans_threads"] * sch1["trans_cols"] > 0
+    assert s1["L"] == s0["L"] and s1["cg"] == s0["cg"] and np.array_equal(X1, X0)
+    _feasible(X1)
+
+
+def test_option_errors(built):
+    import pqdts_gb300 as pq
+
+    with pq.Solver(0) as s:
+        with pytest.raises(pq.PqdtsError):
+            s.set_option("no_such_option", 1)
+        with pytest.raises(pq.PqdtsError):
+            s.get_option("sched.nothing")
+        assert s.get_option("graphs") == 1 and s.get_option("autotune") == 1
