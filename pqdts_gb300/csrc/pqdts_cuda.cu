@@ -30,6 +30,7 @@
 #include "fortran_io.h"
 #include "kernels.cuh"
 #include "problem_host.h"
+#include "tc_band.cuh"
 
 namespace pqdts {
 
@@ -241,6 +242,18 @@ struct Schedule {
   int trans_threads = 0;  // FP64 F^T product: threads per row block (0 = heuristic)
   int trans_cols = 0;     // ... and columns per thread
   int tuned = 0;          // 1 = picked by timing, 0 = heuristic
+  int tc = 0;             // mixed CG products on the tensor cores (split-BF16x3)
+  int tc_splits = 1;      // K segments of their F^T product
+};
+
+// Band operand of the tensor-core products: 128-row blocks of bf16 hi/lo
+// values, block b covering K columns [kb[b], kb[b] + 64 nch[b]), with the
+// TMA maps of both halves (box 64 K x 128 rows, 128-byte swizzle).
+struct TcOperand {
+  DBuf<__nv_bfloat16> hi, lo;
+  DBuf<int32_t> kb, nch;
+  int blocks = 0, kmax = 0;
+  CUtensorMap map_hi, map_lo;
 };
 
 // CG work vectors of one precision.
@@ -314,6 +327,15 @@ struct pqdts_ctx {
   std::map<std::array<uint64_t, 5>, pqdts::CGGraph> graphs;
   bool use_graphs = true;
   bool autotune = true;
+  // tensor-core Hessian products of the mixed CG: option (-1 auto, 0 off,
+  // 1 on), operands F and F^T, the split B operands V^T and (2 F.V)^T
+  int tc_option = 0;
+  bool tc_ready = false;
+  int tc_bn = 0, tc_stages = 0;
+  int64_t tc_mp = 0, tc_dp = 0;  // row strides (elements) of V^T and (F.V)^T
+  pqdts::TcOperand tcF, tcFt;
+  pqdts::DBuf<__nv_bfloat16> vt_hi, vt_lo, yt_hi, yt_lo;
+  CUtensorMap map_vt_hi, map_vt_lo, map_yt_hi, map_yt_lo;
   pqdts::Schedule sched;
   void drop_graphs() noexcept {
     for (auto& kv : graphs) kv.second.destroy();
@@ -436,6 +458,7 @@ static void setup_device(Ctx& c) {
   c.ipart.alloc(kElemGrid);
   c.icount.alloc(1);
   c.sc.alloc(SC_NSC);
+  CK(cudaMemsetAsync(c.sc.p, 0, SC_NSC * sizeof(double), c.st));
   c.alphas.alloc(kBatchLS);
   c.lsout.alloc(4 * kBatchLS);
   c.cglog.alloc(4 * kMaxCG);
@@ -698,6 +721,158 @@ static void hvp(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, const int8_t* ik
   if (with_dot) reduce_to(c, c.part.p, M, c.sc.p + SC_V2, 1, false, 0.0, pred);
 }
 
+// ---------------------------------------------------------------------------
+// Tensor-core (tcgen05 + TMA, split-BF16x3) Hessian products of the mixed CG.
+// ---------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled from the driver (no link-time libcuda dependency).
+static EncodeTiledFn encode_tiled() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  });
+  if (!fn) throw Err(PQDTS_E_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  return fn;
+}
+
+// 2-D bf16 map: inner x outer elements, rows row_bytes apart, box
+// box_inner x box_outer, 128-byte swizzle, zero fill outside the extents.
+static void make_map_bf16(CUtensorMap* m, const void* base, uint64_t inner, uint64_t outer, uint64_t row_bytes,
+                          uint32_t box_inner, uint32_t box_outer) {
+  const cuuint64_t dims[2] = {inner, outer};
+  const cuuint64_t strides[1] = {row_bytes};
+  const cuuint32_t box[2] = {box_inner, box_outer};
+  const cuuint32_t es[2] = {1, 1};
+  const CUresult r = encode_tiled()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box,
+                                    es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw Err(PQDTS_E_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+}
+
+// Band rows (lo / w / off / val over R rows, FP64) as a TcOperand: values
+// split into bf16 hi + lo (hi = bf16(v), lo = bf16(v - hi)).
+static void build_tc_operand(Ctx& c, const std::vector<int32_t>& lo, const std::vector<int32_t>& w,
+                             const std::vector<int64_t>& off, const std::vector<double>& val, int64_t R,
+                             TcOperand& op) {
+  const int blocks = cdiv(R, kTcRows);
+  std::vector<int32_t> kb(blocks, -1), nch(blocks, 0);
+  int kmax = kTcK;
+  for (int b = 0; b < blocks; ++b) {
+    int64_t k0 = INT64_MAX, k1 = -1;
+    const int64_t r1 = std::min<int64_t>(R, (int64_t)(b + 1) * kTcRows);
+    for (int64_t r = (int64_t)b * kTcRows; r < r1; ++r)
+      if (w[r] > 0) {
+        k0 = std::min<int64_t>(k0, lo[r]);
+        k1 = std::max<int64_t>(k1, (int64_t)lo[r] + w[r]);
+      }
+    if (k1 < 0) continue;
+    kb[b] = (int32_t)(k0 / kTcK * kTcK);
+    nch[b] = (int32_t)((k1 - kb[b] + kTcK - 1) / kTcK);
+    kmax = std::max(kmax, nch[b] * kTcK);
+  }
+  const size_t total = (size_t)blocks * kTcRows * kmax;
+  std::vector<__nv_bfloat16> hv(total, __float2bfloat16(0.0f)), lv(total, __float2bfloat16(0.0f));
+  for (int64_t r = 0; r < R; ++r) {
+    const int b = (int)(r / kTcRows);
+    for (int k = 0; k < w[r]; ++k) {
+      const size_t x = (size_t)r * kmax + (size_t)(lo[r] + k - kb[b]);
+      const double v = val[off[r] + k];
+      const __nv_bfloat16 h = __double2bfloat16(v);
+      hv[x] = h;
+      lv[x] = __double2bfloat16(v - (double)__bfloat162float(h));
+    }
+  }
+  op.hi.upload(hv.data(), total, c.st, &c.h2d);
+  op.lo.upload(lv.data(), total, c.st, &c.h2d);
+  op.kb.upload(kb.data(), blocks, c.st, &c.h2d);
+  op.nch.upload(nch.data(), blocks, c.st, &c.h2d);
+  op.blocks = blocks;
+  op.kmax = kmax;
+  make_map_bf16(&op.map_hi, op.hi.p, kmax, (uint64_t)blocks * kTcRows, (uint64_t)kmax * 2, kTcK, kTcRows);
+  make_map_bf16(&op.map_lo, op.lo.p, kmax, (uint64_t)blocks * kTcRows, (uint64_t)kmax * 2, kTcK, kTcRows);
+  CK(cudaStreamSynchronize(c.st));  // the host staging vectors go out of scope
+}
+
+// Tile width over N: N split in ceil(N/256) equal tiles, rounded up to 16
+// (MMA N for M = 128: 16..256 in steps of 16).
+static int tc_tile_n(int64_t N) {
+  const int64_t nt = (N + 255) / 256;
+  const int64_t bn = ((N + nt - 1) / nt + 15) / 16 * 16;
+  return (int)std::max<int64_t>(16, std::min<int64_t>(256, bn));
+}
+
+static uint32_t tc_stage_bytes(int bn) { return 2u * kTcRows * 128u + 2u * (uint32_t)bn * 128u; }
+
+// Operands and maps of the tensor-core products (mixed precision, when the
+// option allows and the device is a tcgen05 part).
+static void setup_tc(Ctx& c) {
+  c.tc_ready = false;
+  if (c.precision != PQDTS_MIXED || c.tc_option == 0) return;
+  int major = 0;
+  CK(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, c.device));
+  if (major != 10) {
+    if (c.tc_option == 1) throw Err(PQDTS_E_ARG, "tensor-core products need a compute capability 10.x device");
+    return;
+  }
+  const HostProblem& h = c.h;
+  const int64_t M = h.M, N = h.N, D = h.D;
+  const int bn = tc_tile_n(N);
+  const uint32_t stage = tc_stage_bytes(bn);
+  const int stages = std::min<int>(kTcMaxStages, (int)((200u * 1024u) / stage));
+  if (stages < 2) throw Err(PQDTS_E_STATE, "internal: tensor-core stage ring does not fit");
+  build_tc_operand(c, h.flo, h.fw, h.foff, h.fval, D, c.tcF);
+  build_tc_operand(c, h.tlo, h.tw, h.toff, h.tbval, M, c.tcFt);
+  c.tc_mp = (M + 7) / 8 * 8;
+  c.tc_dp = (D + 7) / 8 * 8;
+  c.vt_hi.alloc((size_t)N * c.tc_mp);
+  c.vt_lo.alloc((size_t)N * c.tc_mp);
+  c.yt_hi.alloc((size_t)N * c.tc_dp);
+  c.yt_lo.alloc((size_t)N * c.tc_dp);
+  make_map_bf16(&c.map_vt_hi, c.vt_hi.p, M, N, (uint64_t)c.tc_mp * 2, kTcK, bn);
+  make_map_bf16(&c.map_vt_lo, c.vt_lo.p, M, N, (uint64_t)c.tc_mp * 2, kTcK, bn);
+  make_map_bf16(&c.map_yt_hi, c.yt_hi.p, D, N, (uint64_t)c.tc_dp * 2, kTcK, bn);
+  make_map_bf16(&c.map_yt_lo, c.yt_lo.p, D, N, (uint64_t)c.tc_dp * 2, kTcK, bn);
+  CK(cudaFuncSetAttribute(k_tc_band, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(stages * stage + 1024)));
+  c.tc_bn = bn;
+  c.tc_stages = stages;
+  c.tc_ready = true;
+}
+
+// Out = scale * A . B^T on the tensor cores (A a TcOperand of R rows; B the
+// K-major split operand behind bhi / blo); mode 0: FP32 partials (splits of
+// the K range, out_stride apart), mode 1: transposed bf16 split into oh / ol.
+static void tc_product(Ctx& c, const TcOperand& A, const CUtensorMap& bhi, const CUtensorMap& blo, int R, int splits,
+                       int mode, float scale, float* out, __nv_bfloat16* oh, __nv_bfloat16* ol, int64_t ld,
+                       const double* pred) {
+  const int N = (int)c.h.N;
+  const dim3 grid(cdiv(N, c.tc_bn), A.blocks, splits);
+  const size_t smem = (size_t)c.tc_stages * tc_stage_bytes(c.tc_bn) + 1024;
+  k_tc_band<<<grid, kTcThreads, smem, c.st>>>(A.map_hi, A.map_lo, bhi, blo, A.kb.p, A.nch.p, R, N, c.tc_bn,
+                                              c.tc_stages, splits, mode, scale, out, (int64_t)R * N, oh, ol, ld, pred,
+                                              c.sc.p + SC_TCERR);
+  post_launch(c);
+}
+
+// The Hessian product pair on the tensor cores: V -> V^T split, then
+// (2 F.V)^T split (written by the first product's epilogue), then the
+// partials of F^T.(2 F.V) in hpart32 (tc_splits of them).
+static void tc_hvp_products(Ctx& c, const float* src, const double* pred) {
+  const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
+  k_split_t<<<dim3(cdiv(M, 32), cdiv(N, 32)), dim3(32, 8), 0, c.st>>>(src, M, N, c.tc_mp, c.vt_hi.p, c.vt_lo.p, pred);
+  post_launch(c);
+  tc_product(c, c.tcF, c.map_vt_hi, c.map_vt_lo, D, 1, 1, 2.0f, nullptr, c.yt_hi.p, c.yt_lo.p, c.tc_dp, pred);
+  tc_product(c, c.tcFt, c.map_yt_hi, c.map_yt_lo, M, c.sched.tc_splits, 0, 1.0f, c.hpart32.p, nullptr, nullptr, 0,
+             pred);
+}
+
 // Out (R x N) = scale * Band (R rows) . In with tile code `tile` (0 = 64x64,
 // 1 = 64x32, 2 = 32x32 rows x columns); grid.z = nz stacked products
 // (in_stride / out_stride apart) or, with splits > 1, the K segments of one
@@ -746,13 +921,19 @@ static int heuristic_tile(int R, int N, int nz = 1) {
 static void hvp32(Ctx& c, CGBufs<float>& b, const int8_t* ik, bool with_dot, const double* pred) {
   const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
   const float* src = c.fullspace ? b.p.p : b.V.p;
-  launch_band_gemm32(c, c.sched.fwd_tile, c.flo.p, c.fw.p, c.foff.p, c.fval32.p, src, D, N, 2.0f, b.R2.p, pred);
-  // F^T.(2O) with its K range split in trn_splits segments; the epilogue
-  // sums the partial products in a fixed order
   require(c.hpart32.p, "split-K partials");
-  const int parts = c.sched.trn_splits;
-  launch_band_gemm32(c, c.sched.trn_tile, c.tlo.p, c.tw.p, c.toff.p, c.tbval32.p, b.R2.p, M, N, 1.0f, c.hpart32.p,
-                     pred, parts, 0, (int64_t)M * N, parts);
+  int parts;
+  if (c.sched.tc) {
+    tc_hvp_products(c, src, pred);
+    parts = c.sched.tc_splits;
+  } else {
+    launch_band_gemm32(c, c.sched.fwd_tile, c.flo.p, c.fw.p, c.foff.p, c.fval32.p, src, D, N, 2.0f, b.R2.p, pred);
+    // F^T.(2O) with its K range split in trn_splits segments; the epilogue
+    // sums the partial products in a fixed order
+    parts = c.sched.trn_splits;
+    launch_band_gemm32(c, c.sched.trn_tile, c.tlo.p, c.tw.p, c.toff.p, c.tbval32.p, b.R2.p, M, N, 1.0f, c.hpart32.p,
+                       pred, parts, 0, (int64_t)M * N, parts);
+  }
   const int tb = std::min(256, std::max(32, cdiv(N, 32) * 32));
   k_hvp_epi32<<<M, tb, 0, c.st>>>(c.hpart32.p, b.p.p, c.fullspace ? nullptr : b.rs.p, c.maxr.p, c.fullspace ? 0 : 1,
                                   (float)(2.0 * c.h.gam), ik, M, N, b.Hp.p, with_dot ? c.part.p : nullptr, pred,
@@ -829,6 +1010,7 @@ static int cg_chunks(Ctx& c, std::array<uint64_t, 4> variant, Iter&& iteration) 
       for (int k = 0; k < chunk && queued < kMaxCG; ++k, ++queued) iteration(queued == 0);
       read_back(c, c.sc.p, SC_NSC);
     }
+    if (c.pin[SC_TCERR] != 0.0) throw Err(PQDTS_E_CUDA, "tensor-core product: a barrier wait timed out");
     if (c.pin[SC_DONE] != 0.0 || queued >= kMaxCG) return (int)c.pin[SC_ITER];
   }
 }
@@ -1448,7 +1630,7 @@ static void solve(Ctx& c, int mode, int maxiiter, double conv_thres, int start_s
 // one bucket (a resampled or gamma-swept batch) are tuned once.
 // ---------------------------------------------------------------------------
 static std::mutex g_sched_mu;
-static std::map<std::array<int64_t, 6>, Schedule> g_sched;
+static std::map<std::array<int64_t, 7>, Schedule> g_sched;
 
 static int ilog2_ceil(int64_t v) {
   int k = 0;
@@ -1538,6 +1720,27 @@ static void tune_schedule(Ctx& c, Schedule& s) {
     }
   }
   if (c.precision != PQDTS_MIXED) return;
+  if (s.tc) {
+    // tensor-core F^T product: K splits of at most 1 GiB of partials
+    const int max_splits = (int)std::max<int64_t>(1, std::min<int64_t>(8, ((int64_t)1 << 30) / (MN * 4)));
+    c.hpart32.alloc((size_t)std::max(max_splits, s.tc_splits) * MN);
+    CK(cudaMemsetAsync(c.yt_hi.p, 0, c.yt_hi.n * sizeof(__nv_bfloat16), c.st));
+    CK(cudaMemsetAsync(c.yt_lo.p, 0, c.yt_lo.n * sizeof(__nv_bfloat16), c.st));
+    auto trn = [&](int sp) {
+      tc_product(c, c.tcFt, c.map_yt_hi, c.map_yt_lo, M, sp, 0, 1.0f, c.hpart32.p, nullptr, nullptr, 0, nullptr);
+    };
+    float best = time_calls(c, kTuneReps, [&] { trn(s.tc_splits); });
+    if (best < kTuneMaxMs)
+      for (int sp : {1, 2, 3, 4, 6, 8}) {
+        if (sp > max_splits || sp == s.tc_splits) continue;
+        const float t = time_calls(c, kTuneReps, [&] { trn(sp); });
+        if (t < best * (sp > s.tc_splits ? 0.97f : 1.0f)) {
+          best = t;
+          s.tc_splits = sp;
+        }
+      }
+    return;
+  }
   CGBufs<float>& b = c.cg32;
   CK(cudaMemsetAsync(b.p.p, 0, b.p.n * sizeof(float), c.st));
   CK(cudaMemsetAsync(b.R2.p, 0, b.R2.n * sizeof(float), c.st));
@@ -1579,10 +1782,17 @@ static void tune_schedule(Ctx& c, Schedule& s) {
 
 static void choose_schedule(Ctx& c) {
   const HostProblem& h = c.h;
+  setup_tc(c);
   Schedule s = heuristic_schedule(h);
+  if (c.tc_ready) {
+    s.tc = 1;
+    const int64_t ctas = (int64_t)cdiv(h.N, c.tc_bn) * c.tcFt.blocks;
+    s.tc_splits = (int)std::min<int64_t>(8, std::max<int64_t>(1, (152 + ctas - 1) / ctas));
+  }
   if (c.autotune) {
     const int64_t wavg = h.D > 0 ? std::max<int64_t>(1, h.nnz() / h.D) : 1;
-    const std::array<int64_t, 6> key{c.device, c.precision, h.N, ilog2_ceil(h.M), ilog2_ceil(h.D), ilog2_ceil(wavg)};
+    const std::array<int64_t, 7> key{c.device,          c.precision,       h.N, ilog2_ceil(h.M), ilog2_ceil(h.D),
+                                     ilog2_ceil(wavg), (int64_t)s.tc};
     std::lock_guard<std::mutex> lk(g_sched_mu);
     auto it = g_sched.find(key);
     if (it != g_sched.end()) {
@@ -1595,12 +1805,13 @@ static void choose_schedule(Ctx& c) {
   }
   c.sched = s;
   if (c.precision == PQDTS_MIXED) {
-    const size_t need = (size_t)s.trn_splits * (size_t)h.M * (size_t)h.N;
+    const size_t need = (size_t)(s.tc ? s.tc_splits : s.trn_splits) * (size_t)h.M * (size_t)h.N;
     if (c.hpart32.n != need) c.hpart32.alloc(need);
   } else {
     c.hpart32.release();
   }
-  CK(cudaStreamSynchronize(c.st));
+  read_back(c, c.sc.p, SC_NSC);
+  if (c.pin[SC_TCERR] != 0.0) throw Err(PQDTS_E_CUDA, "tensor-core product: a barrier wait timed out");
 }
 
 // Problem set-up shared by the entry points.
@@ -1899,7 +2110,8 @@ int pqdts_cuda_BF32(pqdts_ctx* c, const double* V, double* HV) {
     }
     pqdts::hvp32(*c, b, nullptr, false, nullptr);
     CK(cudaMemcpyAsync(rm.data(), b.Hp.p, rm.size() * 4, cudaMemcpyDeviceToHost, c->st));
-    CK(cudaStreamSynchronize(c->st));
+    pqdts::read_back(*c, c->sc.p, pqdts::SC_NSC);
+    if (c->pin[pqdts::SC_TCERR] != 0.0) throw Err(PQDTS_E_CUDA, "tensor-core product: a barrier wait timed out");
     c->d2h += (int64_t)rm.size() * 4;
     for (int64_t i = 0; i < M; ++i)
       for (int64_t n = 0; n < N; ++n) HV[i + n * M] = rm[(size_t)i * N + n];
@@ -2041,6 +2253,9 @@ int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
       c->use_graphs = value != 0;
     } else if (n == "autotune") {
       c->autotune = value != 0;
+    } else if (n == "tensor_cores") {
+      if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "tensor_cores must be -1, 0 or 1");
+      c->tc_option = (int)value;
     } else {
       throw pqdts::Err(PQDTS_E_ARG, "unknown option " + n);
     }
@@ -2060,6 +2275,9 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     else if (n == "sched.trans_threads") *value = s.trans_threads;
     else if (n == "sched.trans_cols") *value = s.trans_cols;
     else if (n == "sched.tuned") *value = s.tuned;
+    else if (n == "sched.tc") *value = s.tc;
+    else if (n == "sched.tc_splits") *value = s.tc_splits;
+    else if (n == "tensor_cores") *value = c->tc_option;
     else if (n == "graphs.captured") *value = (int64_t)c->graphs.size();
     else throw pqdts::Err(PQDTS_E_ARG, "unknown option " + n);
   });

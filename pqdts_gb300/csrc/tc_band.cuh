@@ -1,0 +1,334 @@
+// Banded products on the 5th-generation tensor cores (tcgen05 + TMA) with
+// split-BF16x3 compensation: every FP32 operand x is held as the bf16 pair
+// hi = bf16(x), lo = bf16(x - hi), and a product a.b is accumulated in FP32
+// as hi_a.hi_b + hi_a.lo_b + lo_a.hi_b (the lo.lo term, ~2^-16 relative,
+// is dropped).  Used for the Hessian-vector products of the mixed-precision
+// CG (BF, pqdts.f90:246-342), whose FP32 accumulation it replaces.
+//
+// Out[r, n] = scale * sum_k Band[r, k] * B[n, k]
+//
+// The band operand is stored in 128-row blocks, each with its own K window
+// [kb, kb + 64*nch) (kb a multiple of 64, zero filled outside the rows'
+// bands): rows r of block b hold Band[r, kb + x] at local column x.  B is
+// N rows of K (K contiguous, "K-major"): V^T for F.V, (2 F.V)^T for F^T.(.).
+// One CTA computes a 128 x BN tile: warp 0 lane 0 streams 64-wide K chunks
+// of A hi/lo and B hi/lo through a ring of shared-memory stages with TMA
+// (128-byte swizzle), warp 1 lane 0 issues the MMAs (M=128, N=BN, K=16,
+// bf16 in, FP32 accumulator in tensor memory), all four warps then read the
+// accumulator back (tcgen05.ld, one row per thread) and store it.
+//
+// Every mbarrier wait is bounded (kTcWaitNs); a wait that runs out sets
+// *err, skips the remaining work and stores nothing.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cstdint>
+
+namespace pqdts {
+
+constexpr int kTcThreads = 128;
+constexpr int kTcRows = 128;           // rows of a band block = MMA M
+constexpr int kTcK = 64;               // K per stage: one 128-byte swizzled row of bf16
+constexpr int kTcMaxStages = 4;
+constexpr uint64_t kTcWaitNs = 2000000000ull;  // 2 s per wait
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.b32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Wait for the phase of `parity` to complete; false when kTcWaitNs ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  while (!mbar_try_wait(bar, parity))
+    if (global_ns() - t0 > kTcWaitNs) return false;
+  return true;
+}
+
+// 2-D TMA tile load (x = inner coordinate, elements) completing on `bar`.
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+          "r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_alloc(uint32_t* dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tc_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// D(tmem) (+)= A(smem) . B(smem)^T, kind::f16 (bf16 inputs, FP32 accumulator).
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                       uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// Arrive on `bar` once all tcgen05 operations issued so far have completed.
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+// 16 consecutive FP32 columns of this thread's accumulator row (32x32b
+// shape: lane t of the warp reads TMEM lane base + t), waited in place.
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// Shared-memory matrix descriptor of a K-major operand tile written by TMA
+// with the 128-byte swizzle: rows of 128 bytes, 8-row groups 1024 bytes
+// apart (stride byte offset), tile base 1024-byte aligned; advancing the
+// start address by 32 bytes selects the next K=16 slice of the swizzled row.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4)  // start address
+         | ((uint64_t)1 << 16)                // leading byte offset (unused for swizzled K-major)
+         | ((uint64_t)(1024 >> 4) << 32)      // stride byte offset
+         | ((uint64_t)1 << 46)                // descriptor version
+         | ((uint64_t)2 << 61);               // 128-byte swizzle
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulator, bf16 A and B, both
+// K-major, M x N.
+__host__ __device__ constexpr uint32_t tc_idesc_bf16(int m, int n) {
+  return (1u << 4)                          // D format: F32
+         | (1u << 7)                        // A format: BF16
+         | (1u << 10)                       // B format: BF16
+         | ((uint32_t)(n >> 3) << 17)       // N / 8
+         | ((uint32_t)(m >> 4) << 24);      // M / 16
+}
+
+__host__ __device__ constexpr uint32_t tc_tmem_cols(int bn) {
+  return bn <= 32 ? 32u : bn <= 64 ? 64u : bn <= 128 ? 128u : 256u;
+}
+
+// mode 0: FP32 Out[z * out_stride + r * N + n] = scale * acc (row-major; z =
+//         the K split whose partial this is).
+// mode 1: Out^T split again: oh[n * ld + r] = hi, ol[n * ld + r] = lo of
+//         scale * acc (the next product's K-major B operand).
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_tc_band(const __grid_constant__ CUtensorMap mA_hi, const __grid_constant__ CUtensorMap mA_lo,
+              const __grid_constant__ CUtensorMap mB_hi, const __grid_constant__ CUtensorMap mB_lo,
+              const int32_t* __restrict__ blk_kb, const int32_t* __restrict__ blk_nch, int R, int N, int BN,
+              int stages, int splits, int mode, float scale, float* __restrict__ out, int64_t out_stride,
+              __nv_bfloat16* __restrict__ oh, __nv_bfloat16* __restrict__ ol, int64_t ld,
+              const double* __restrict__ pred, double* __restrict__ err) {
+  if (pred != nullptr && pred[6] != 0.0) return;  // CG already converged
+  extern __shared__ uint8_t tc_smem_raw[];
+  __shared__ uint64_t bar_full[kTcMaxStages], bar_empty[kTcMaxStages], bar_acc;
+  __shared__ uint32_t s_tmem;
+  __shared__ volatile int s_abort;
+  __shared__ int s_issued, s_consumed;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int blk = blockIdx.y, n0 = blockIdx.x * BN, r0 = blk * kTcRows;
+  const int kb = blk_kb[blk];
+  int c0 = 0, c1 = kb >= 0 ? blk_nch[blk] : 0;
+  if (splits > 1) {  // this CTA's share of the block's K chunks
+    const int per = (c1 + splits - 1) / splits;
+    c0 = min(c1, (int)blockIdx.z * per);
+    c1 = min(c1, c0 + per);
+  }
+  const int nk = c1 - c0;
+
+  // stage ring, 1024-byte aligned (swizzle atoms)
+  const uint32_t raw = smem_u32(tc_smem_raw);
+  uint8_t* base = tc_smem_raw + ((1024u - (raw & 1023u)) & 1023u);
+  const uint32_t a_bytes = kTcRows * 128u, b_bytes = (uint32_t)BN * 128u;
+  const uint32_t stage_bytes = 2u * a_bytes + 2u * b_bytes;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < stages; ++i) {
+      mbar_init(&bar_full[i], 1);
+      mbar_init(&bar_empty[i], 1);
+    }
+    mbar_init(&bar_acc, 1);
+    s_abort = 0;
+    s_issued = 0;
+    s_consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  const uint32_t ncols = tc_tmem_cols(BN);
+  if (warp == 0) {
+    tc_alloc(&s_tmem, ncols);
+    tc_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = s_tmem;
+
+  if (warp == 0 && lane == 0 && nk > 0) {
+    // producer: TMA loads of A hi/lo (block-local K) and B hi/lo (global K)
+    for (int it = 0; it < nk && !s_abort; ++it) {
+      const int st = it % stages;
+      const uint32_t ph = (uint32_t)(it / stages) & 1u;
+      if (!mbar_wait(&bar_empty[st], ph ^ 1u)) {
+        s_abort = 1;
+        break;
+      }
+      uint8_t* sa = base + (size_t)st * stage_bytes;
+      uint8_t* sb = sa + 2 * a_bytes;
+      mbar_expect_tx(&bar_full[st], stage_bytes);
+      const int kx = (c0 + it) * kTcK;
+      tma_load_2d(sa, &mA_hi, kx, r0, &bar_full[st]);
+      tma_load_2d(sa + a_bytes, &mA_lo, kx, r0, &bar_full[st]);
+      tma_load_2d(sb, &mB_hi, kb + kx, n0, &bar_full[st]);
+      tma_load_2d(sb + b_bytes, &mB_lo, kb + kx, n0, &bar_full[st]);
+      s_issued = it + 1;
+    }
+  } else if (warp == 1 && lane == 0 && nk > 0) {
+    // MMA issuer: 4 K-slices of 16 x 3 compensated terms per stage
+    const uint32_t idesc = tc_idesc_bf16(kTcRows, BN);
+    for (int it = 0; it < nk && !s_abort; ++it) {
+      const int st = it % stages;
+      const uint32_t ph = (uint32_t)(it / stages) & 1u;
+      if (!mbar_wait(&bar_full[st], ph)) {
+        s_abort = 1;
+        break;
+      }
+      s_consumed = it + 1;
+      tc_fence_after();
+      const uint32_t a_hi = smem_u32(base + (size_t)st * stage_bytes);
+      const uint32_t a_lo = a_hi + a_bytes, b_hi = a_hi + 2 * a_bytes, b_lo = b_hi + b_bytes;
+#pragma unroll
+      for (int k = 0; k < kTcK / 16; ++k) {
+        const uint32_t o = 32u * k;
+        tc_mma(tmem, sw128_desc(a_lo + o), sw128_desc(b_hi + o), idesc, (it > 0 || k > 0) ? 1u : 0u);
+        tc_mma(tmem, sw128_desc(a_hi + o), sw128_desc(b_lo + o), idesc, 1u);
+        tc_mma(tmem, sw128_desc(a_hi + o), sw128_desc(b_hi + o), idesc, 1u);
+      }
+      tc_commit(&bar_empty[st]);  // the stage is free once these MMAs are done
+    }
+    tc_commit(&bar_acc);
+  }
+  __syncwarp();
+
+  // epilogue: thread t of warp w owns accumulator row 32w + t
+  bool ok = true;
+  if (nk > 0) {
+    ok = mbar_wait(&bar_acc, 0);
+    tc_fence_after();
+  }
+  if (!ok) s_abort = 1;
+  const int r = r0 + warp * 32 + lane;
+  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+  for (int cc = 0; cc < BN; cc += 16) {
+    float v[16];
+    if (nk > 0) {
+      tc_ld16(trow + (uint32_t)cc, v);
+    } else {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) v[j] = 0.f;
+    }
+    const bool store = !s_abort && r < R;  // (the loads above stay warp-converged)
+    if (!store) {
+    } else if (mode == 0) {
+      float* o = out + (int64_t)blockIdx.z * out_stride + (int64_t)r * N;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int n = n0 + cc + j;
+        if (n < N) o[n] = scale * v[j];
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int n = n0 + cc + j;
+        if (n < N) {
+          const float x = scale * v[j];
+          const __nv_bfloat16 h = __float2bfloat16_rn(x);
+          oh[(int64_t)n * ld + r] = h;
+          ol[(int64_t)n * ld + r] = __float2bfloat16_rn(x - __bfloat162float(h));
+        }
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (s_abort && threadIdx.x == 0) {
+    *err = 1.0;
+    // let the copies already in flight land before the CTA's memory goes
+    for (int it = s_consumed; it < s_issued; ++it)
+      if (!mbar_wait(&bar_full[it % stages], (uint32_t)(it / stages) & 1u)) break;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tc_dealloc(tmem, ncols);
+  }
+}
+
+// V (M x N row-major FP32) -> V^T split: hi[n * ld + i], lo[n * ld + i].
+__global__ void k_split_t(const float* __restrict__ V, int M, int N, int64_t ld, __nv_bfloat16* __restrict__ hi,
+                          __nv_bfloat16* __restrict__ lo, const double* __restrict__ pred) {
+  if (pred != nullptr && pred[6] != 0.0) return;
+  __shared__ float t[32][33];
+  const int i0 = blockIdx.x * 32, n0 = blockIdx.y * 32;
+  for (int rr = threadIdx.y; rr < 32; rr += blockDim.y) {
+    const int i = i0 + rr, n = n0 + threadIdx.x;
+    t[rr][threadIdx.x] = (i < M && n < N) ? V[(int64_t)i * N + n] : 0.f;
+  }
+  __syncthreads();
+  for (int rr = threadIdx.y; rr < 32; rr += blockDim.y) {
+    const int n = n0 + rr, i = i0 + threadIdx.x;
+    if (n < N && i < M) {
+      const float x = t[threadIdx.x][rr];
+      const __nv_bfloat16 h = __float2bfloat16_rn(x);
+      hi[(int64_t)n * ld + i] = h;
+      lo[(int64_t)n * ld + i] = __float2bfloat16_rn(x - __bfloat162float(h));
+    }
+  }
+}
+
+}  // namespace pqdts

@@ -133,13 +133,24 @@ def det_log_factorial(i):
     return out
 
 
-def poisson_bands(M: int, D: int, xmax: float, cutoff: float = CUTOFF):
-    """Row windows of F[d, i] = Poisson pmf(i; x_d), x_d = linspace(0.01, xmax, D)."""
+def poisson_bands(M: int, D: int, xmax: float, cutoff: float = CUTOFF, dense: bool = False):
+    """Row windows of F[d, i] = Poisson pmf(i; x_d), x_d = linspace(0.01, xmax, D).
+    dense=True keeps every entry (each row spans all M columns)."""
     x = np.linspace(0.01, xmax, D)
     lo = np.full(D, -1, dtype=np.int64)
     hi = np.full(D, -1, dtype=np.int64)
     vals = []
     logx = det_log(x)
+    if dense:
+        ii = np.arange(M, dtype=np.int64)
+        lf = det_log_factorial(ii)
+        for d0 in range(0, D, 256):
+            d1 = min(D, d0 + 256)
+            t = ii[None, :] * logx[d0:d1, None] - x[d0:d1, None] - lf[None, :]
+            vals.append(det_exp(np.maximum(t, -745.0)).ravel())
+        lo[:] = 0
+        hi[:] = M - 1
+        return lo, hi, np.concatenate(vals)
     for d in range(D):
         xd = float(x[d])
         half = 12.0 * math.sqrt(xd) + 40.0
@@ -194,9 +205,9 @@ def sample_P(FPi: np.ndarray, shots: int, rng: np.random.Generator) -> np.ndarra
     return counts.astype(np.float64) / float(shots)
 
 
-def make_instance(M, N, D, xmax, eta, shots, gamma, eps, seed=0, keep_truth=False) -> Instance:
+def make_instance(M, N, D, xmax, eta, shots, gamma, eps, seed=0, keep_truth=False, dense=False) -> Instance:
     rng = np.random.default_rng(seed)
-    lo, hi, val = poisson_bands(M, D, xmax)
+    lo, hi, val = poisson_bands(M, D, xmax, dense=dense)
     pi = binomial_povm(M, N, eta)
     P = sample_P(band_matvec(lo, hi, val, pi), shots, rng)
     return Instance(M, N, D, gamma, eps, lo, hi, val, P, pi if keep_truth else None)
