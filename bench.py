@@ -383,15 +383,28 @@ def run_ours(args):
     # time to an objective within 1e-8 relative of L64
     extra = {}
     if prec == pq.FP64 and args.with_mixed and world == 1:
-        with pq.Solver(local) as sm:
-            sm.set_instance(inst, pq.MIXED)
-            timed_solves(sm, args.warmup, 1e-300, target)
-            mt, ms = timed_solves(sm, args.steps, 1e-300, target)
-            mval = statistics.mean(mt)
-            extra["mixed"] = {"value": mval, "unit": "s", "speedup_vs_fp64": step_s / mval,
-                              "stop": "objective <= L64*(1+1e-8)", "objective": ms[-1]["L"],
-                              "rel_obj_vs_L64": (ms[-1]["L"] - L64) / L64, "reached": ms[-1]["L"] <= target,
-                              "outer": ms[-1]["outer"], "cg": ms[-1]["cg"], "refine": ms[-1]["refine"]}
+        def mixed_run(tc):
+            with pq.Solver(local) as sm:
+                sm.set_option("tensor_cores", tc)
+                sm.set_instance(inst, pq.MIXED)
+                timed_solves(sm, args.warmup, 1e-300, target)
+                b0 = sm.timer("BF")
+                mt, ms = timed_solves(sm, args.steps, 1e-300, target)
+                b1 = sm.timer("BF")
+                mval = statistics.mean(mt)
+                cgs = sum(x["cg"] for x in ms)
+                bft = b1[0] - b0[0]
+                out = {"value": mval, "unit": "s", "speedup_vs_fp64": step_s / mval,
+                       "stop": "objective <= L64*(1+1e-8)", "objective": ms[-1]["L"],
+                       "rel_obj_vs_L64": (ms[-1]["L"] - L64) / L64, "reached": ms[-1]["L"] <= target,
+                       "outer": ms[-1]["outer"], "cg": ms[-1]["cg"], "refine": ms[-1]["refine"],
+                       "tensor_cores": bool(sm.get_option("sched.tc")),
+                       "hessian_product_pair": {"us_per_cg_iteration": bft / cgs * 1e6 if cgs else None,
+                                                "algorithmic_tflops": flops_pair * cgs / bft / 1e12 if bft else None}}
+                return out
+        extra["mixed"] = mixed_run(-1)
+        if extra["mixed"]["tensor_cores"]:
+            extra["mixed"]["cuda_core_variant"] = mixed_run(0)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -441,6 +454,20 @@ def run_profile_case(case):
     import pqdts_gb300 as pq
     from pqdts_gb300 import synth
 
+    if case in ("tc3", "tcdense"):
+        # the tensor-core Hessian product pair (3 BF32 calls, no autotuning
+        # launches) at M=10000 N=1000 D=20000, or on the dense-F variant
+        inst = synth.make_config(3 if case == "tc3" else 6, seed=0)
+        with pq.Solver(0) as s:
+            s.set_option("autotune", 0)
+            s.set_instance(inst, pq.MIXED)
+            assert s.get_option("sched.tc") == 1
+            rng = np.random.default_rng(0)
+            V = rng.standard_normal((inst.M, inst.N))
+            for _ in range(3):
+                s.BF32(V)
+            print(json.dumps({"profile_case": case, "launches": s.kernel_launches(), "nnz": inst.nnz}))
+        return 0
     inst = synth.make_config(CONFIG, seed=0)
     prec = pq.MIXED if case in ("mixed", "solvemix") else pq.FP64
     with pq.Solver(0) as s:
@@ -480,8 +507,9 @@ def run_workload(name, args):
                  reference's stopping rule conv < 1e-6, then mixed precision
                  to within 1e-8 relative of each FP64 objective (optionally
                  the FP64 solves one after another for comparison);
-      config3 -- M=10000, N=1000, D=20000: FP64 vs mixed seconds per outer
-                 iteration over the first iterations of each stage."""
+      config3 -- M=10000, N=1000, D=20000: FP64 vs mixed (tensor-core and
+                 CUDA-core Hessian products) over the first outer iterations;
+      dense   -- the same on the dense-F variant M=D=8192, N=256."""
     import numpy as np
 
     import pqdts_gb300 as pq
@@ -522,20 +550,28 @@ def run_workload(name, args):
             out["fp64"]["identical_objectives"] = bool(np.array_equal(np.array(Ls), L64))
         print(json.dumps(out))
         return 0
-    if name == "config3":
-        inst = synth.make_config(3, seed=0)
-        out = {"workload": "M=10000 N=1000 D=20000", "nnz_F": inst.nnz}
-        for prec, tag in ((pq.FP64, "fp64"), (pq.MIXED, "mixed")):
+    if name in ("config3", "dense"):
+        cfg = 3 if name == "config3" else 6
+        inst = synth.make_config(cfg, seed=0)
+        out = {"workload": ("M=10000 N=1000 D=20000 (banded F)" if cfg == 3 else
+                            "M=8192 N=256 D=8192 (dense F, every entry kept)"), "nnz_F": inst.nnz,
+               "iterations": args.config3_iters}
+        flops_pair = 2 * 2.0 * inst.nnz * inst.N
+        for prec, tc, tag in ((pq.FP64, 0, "fp64"), (pq.MIXED, -1, "mixed_tc"), (pq.MIXED, 0, "mixed_cuda_cores")):
             with pq.Solver(0) as s:
+                s.set_option("tensor_cores", tc)
                 s.set_instance(inst, prec)
                 s.init_x()
                 t0 = time.perf_counter()
                 st = s.solve(mode=2, maxiter=args.config3_iters, eps=EPS)
                 el = time.perf_counter() - t0
                 bf = s.timer("BF")
-            out[tag] = {"seconds": el, "outer": st["outer"], "cg": st["cg"], "s_per_outer": el / max(1, st["outer"]),
-                        "L": st["L"], "bf_seconds": bf[0], "bf_calls": bf[1],
-                        "bf_tflops": 2 * 2.0 * inst.nnz * inst.N * st["cg"] / bf[0] / 1e12 if bf[0] else None}
+                out[tag] = {"seconds": el, "outer": st["outer"], "cg": st["cg"],
+                            "s_per_outer": el / max(1, st["outer"]), "L": st["L"],
+                            "tensor_cores": bool(s.get_option("sched.tc")) if prec == pq.MIXED else False,
+                            "bf_seconds": bf[0], "bf_calls": bf[1],
+                            "bf_us_per_call": bf[0] / bf[1] * 1e6 if bf[1] else None,
+                            "bf_tflops_algorithmic": flops_pair * st["cg"] / bf[0] / 1e12 if bf[0] else None}
         print(json.dumps(out))
         return 0
     raise SystemExit("unknown workload " + name)
@@ -553,9 +589,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-iters", type=int, default=4)
     ap.add_argument("--ref-sample-iters", type=int, default=3)
-    ap.add_argument("--profile-case", choices=["fp64", "mixed", "solve64", "solvemix"], default=None,
+    ap.add_argument("--profile-case", choices=["fp64", "mixed", "solve64", "solvemix", "tc3", "tcdense"], default=None,
                     help="launches of the workload for ncu (see run_profile_case)")
-    ap.add_argument("--workload", choices=["batch", "config3"], default=None,
+    ap.add_argument("--workload", choices=["batch", "config3", "dense"], default=None,
                     help="secondary measurement instead of the bench line")
     ap.add_argument("--batch-maxiter", type=int, default=200)
     ap.add_argument("--batch-sequential", action="store_true",

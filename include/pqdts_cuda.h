@@ -55,13 +55,19 @@ int pqdts_cuda_kernel_launches(pqdts_ctx* ctx, int64_t* count);
  *   "autotune" 1 (default): the banded products' launch schedule is timed on
  *              the problem at set-up (once per size bucket per process);
  *              0: heuristic shapes.  Takes effect at the next set_problem.
+ *   "tensor_cores" -1 (default, auto) / 1: the mixed CG's Hessian products
+ *              run on the tensor cores (tcgen05, split-BF16x3, FP32
+ *              accumulation) on compute capability 10.x devices; 0: FP32
+ *              CUDA-core tiles.  Takes effect at the next set_problem.
  * Unknown names return PQDTS_E_ARG. */
 int pqdts_cuda_set_option(pqdts_ctx* ctx, const char* name, int64_t value);
 /* Reads an option above or a field of the schedule in use:
  * "sched.fwd_tile", "sched.trn_tile" (0 = 64x64, 1 = 64x32, 2 = 32x32 FP32
  * tiles of F.V and F^T.R), "sched.trn_splits" (K segments of F^T.R),
  * "sched.trans_threads", "sched.trans_cols" (FP64 F^T product block shape),
- * "sched.tuned" (1 = timed, 0 = heuristic), "graphs.captured" (graphs held). */
+ * "sched.tuned" (1 = timed, 0 = heuristic), "sched.tc" (1 = tensor-core
+ * Hessian products in use), "sched.tc_splits" (K segments of their F^T
+ * product), "graphs.captured" (graphs held). */
 int pqdts_cuda_get_option(pqdts_ctx* ctx, const char* name, int64_t* value);
 /* verbose = 1 prints the reference's stdout lines (iter, newton-pcg, line
  * search, positivity constraints) exactly as rank 0 of pqdts_omp.x. */

@@ -329,7 +329,7 @@ struct pqdts_ctx {
   bool autotune = true;
   // tensor-core Hessian products of the mixed CG: option (-1 auto, 0 off,
   // 1 on), operands F and F^T, the split B operands V^T and (2 F.V)^T
-  int tc_option = 0;
+  int tc_option = -1;
   bool tc_ready = false;
   int tc_bn = 0, tc_stages = 0;
   int64_t tc_mp = 0, tc_dp = 0;  // row strides (elements) of V^T and (F.V)^T

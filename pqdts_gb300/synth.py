@@ -36,6 +36,9 @@ CONFIGS = {
     2: dict(M=2000, N=200, D=4000, xmax=1800.0, eta=0.9, shots=10**7, gamma=1e-5, eps=1e-6),
     3: dict(M=10000, N=1000, D=20000, xmax=9000.0, eta=0.75, shots=10**8, gamma=1e-6, eps=1e-6),
     5: dict(M=50000, N=5000, D=100000, xmax=45000.0, eta=0.85, shots=10**8, gamma=1e-6, eps=1e-6),
+    # configuration 5's dense-F variant: every entry of F kept (N, x_max, eta
+    # are this generator's choice)
+    6: dict(M=8192, N=256, D=8192, xmax=7373.0, eta=0.85, shots=10**8, gamma=1e-6, eps=1e-6, dense=True),
 }
 
 
