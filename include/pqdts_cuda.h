@@ -66,8 +66,9 @@ int pqdts_cuda_set_option(pqdts_ctx* ctx, const char* name, int64_t value);
  * tiles of F.V and F^T.R), "sched.trn_splits" (K segments of F^T.R),
  * "sched.trans_threads", "sched.trans_cols" (FP64 F^T product block shape),
  * "sched.tuned" (1 = timed, 0 = heuristic), "sched.tc" (1 = tensor-core
- * Hessian products in use), "sched.tc_splits" (K segments of their F^T
- * product), "graphs.captured" (graphs held). */
+ * Hessian products in use), "sched.tc_bn" (their N tile width),
+ * "sched.tc_splits" (K segments of their F^T product), "graphs.captured"
+ * (graphs held). */
 int pqdts_cuda_get_option(pqdts_ctx* ctx, const char* name, int64_t* value);
 /* verbose = 1 prints the reference's stdout lines (iter, newton-pcg, line
  * search, positivity constraints) exactly as rank 0 of pqdts_omp.x. */

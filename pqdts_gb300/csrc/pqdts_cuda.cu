@@ -244,6 +244,7 @@ struct Schedule {
   int tuned = 0;          // 1 = picked by timing, 0 = heuristic
   int tc = 0;             // mixed CG products on the tensor cores (split-BF16x3)
   int tc_splits = 1;      // K segments of their F^T product
+  int tc_bn = 0;          // their N tile width
 };
 
 // Band operand of the tensor-core products: 128-row blocks of bf16 hi/lo
@@ -322,6 +323,12 @@ struct pqdts_ctx {
   bool G_full = true;
   double L_cache = 0.0, Lgam_cache = 0.0;  // L of X (version L_ver) and its gamma term
   bool target_hit = false;
+  // last batch of FP64-evaluated line-search candidates (Xc, Rst = O - P):
+  // step lengths, objectives (+ gamma part), xmin, for X of version cand_xver
+  int64_t cand_xver = -1;
+  int cand_B = 0;
+  bool cand_stage2 = false;
+  double cand_alpha[8], cand_L[8], cand_Lgam[8], cand_xmin[8];
   // CG chunks captured as CUDA graphs (keyed by variant; dropped whenever the
   // device buffers are reallocated) and the products' launch schedule
   std::map<std::array<uint64_t, 5>, pqdts::CGGraph> graphs;
@@ -801,15 +808,31 @@ static void build_tc_operand(Ctx& c, const std::vector<int32_t>& lo, const std::
   CK(cudaStreamSynchronize(c.st));  // the host staging vectors go out of scope
 }
 
-// Tile width over N: N split in ceil(N/256) equal tiles, rounded up to 16
-// (MMA N for M = 128: 16..256 in steps of 16).
-static int tc_tile_n(int64_t N) {
-  const int64_t nt = (N + 255) / 256;
+// Tile width over N: N split in mult * ceil(N/256) equal tiles, rounded up
+// to 16 (MMA N for M = 128: 16..256 in steps of 16).
+static int tc_tile_n(int64_t N, int mult) {
+  const int64_t nt = (N + 255) / 256 * mult;
   const int64_t bn = ((N + nt - 1) / nt + 15) / 16 * 16;
   return (int)std::max<int64_t>(16, std::min<int64_t>(256, bn));
 }
 
 static uint32_t tc_stage_bytes(int bn) { return 2u * kTcRows * 128u + 2u * (uint32_t)bn * 128u; }
+constexpr uint32_t kTcRing = 200u * 1024u;           // stage ring budget
+constexpr uint32_t kTcMaxSmem = kTcRing + 1024u;      // + alignment slack
+
+// Tile width BN of the tensor-core products: the B operands' maps (box
+// 64 x BN) and the stage count follow it.
+static void tc_configure(Ctx& c, int bn) {
+  const int64_t M = c.h.M, N = c.h.N, D = c.h.D;
+  const int stages = std::min<int>(kTcMaxStages, (int)(kTcRing / tc_stage_bytes(bn)));
+  if (stages < 2) throw Err(PQDTS_E_STATE, "internal: tensor-core stage ring does not fit");
+  make_map_bf16(&c.map_vt_hi, c.vt_hi.p, M, N, (uint64_t)c.tc_mp * 2, kTcK, bn);
+  make_map_bf16(&c.map_vt_lo, c.vt_lo.p, M, N, (uint64_t)c.tc_mp * 2, kTcK, bn);
+  make_map_bf16(&c.map_yt_hi, c.yt_hi.p, D, N, (uint64_t)c.tc_dp * 2, kTcK, bn);
+  make_map_bf16(&c.map_yt_lo, c.yt_lo.p, D, N, (uint64_t)c.tc_dp * 2, kTcK, bn);
+  c.tc_bn = bn;
+  c.tc_stages = stages;
+}
 
 // Operands and maps of the tensor-core products (mixed precision, when the
 // option allows and the device is a tcgen05 part).
@@ -824,10 +847,7 @@ static void setup_tc(Ctx& c) {
   }
   const HostProblem& h = c.h;
   const int64_t M = h.M, N = h.N, D = h.D;
-  const int bn = tc_tile_n(N);
-  const uint32_t stage = tc_stage_bytes(bn);
-  const int stages = std::min<int>(kTcMaxStages, (int)((200u * 1024u) / stage));
-  if (stages < 2) throw Err(PQDTS_E_STATE, "internal: tensor-core stage ring does not fit");
+  const int bn = tc_tile_n(N, 1);
   build_tc_operand(c, h.flo, h.fw, h.foff, h.fval, D, c.tcF);
   build_tc_operand(c, h.tlo, h.tw, h.toff, h.tbval, M, c.tcFt);
   c.tc_mp = (M + 7) / 8 * 8;
@@ -836,13 +856,8 @@ static void setup_tc(Ctx& c) {
   c.vt_lo.alloc((size_t)N * c.tc_mp);
   c.yt_hi.alloc((size_t)N * c.tc_dp);
   c.yt_lo.alloc((size_t)N * c.tc_dp);
-  make_map_bf16(&c.map_vt_hi, c.vt_hi.p, M, N, (uint64_t)c.tc_mp * 2, kTcK, bn);
-  make_map_bf16(&c.map_vt_lo, c.vt_lo.p, M, N, (uint64_t)c.tc_mp * 2, kTcK, bn);
-  make_map_bf16(&c.map_yt_hi, c.yt_hi.p, D, N, (uint64_t)c.tc_dp * 2, kTcK, bn);
-  make_map_bf16(&c.map_yt_lo, c.yt_lo.p, D, N, (uint64_t)c.tc_dp * 2, kTcK, bn);
-  CK(cudaFuncSetAttribute(k_tc_band, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(stages * stage + 1024)));
-  c.tc_bn = bn;
-  c.tc_stages = stages;
+  CK(cudaFuncSetAttribute(k_tc_band, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcMaxSmem));
+  tc_configure(c, bn);
   c.tc_ready = true;
 }
 
@@ -1213,6 +1228,17 @@ static void eval_candidates(Ctx& c, const double* al, int B, bool stage2, double
   fetch_objectives(c, B, L);
   for (int b = 0; b < B; ++b) xmin[b] = stage2 ? c.pin[2 * kBatchLS + b] : 0.0;
   c.n_lsL += B;
+  // this batch stays in Xc / Rst until the next one: the mixed path adopts
+  // the chosen candidate as the new iterate instead of recomputing it
+  c.cand_xver = c.xver;
+  c.cand_B = B;
+  c.cand_stage2 = stage2;
+  for (int b = 0; b < B; ++b) {
+    c.cand_alpha[b] = al[b];
+    c.cand_L[b] = L[b];
+    c.cand_Lgam[b] = (c.h.gam != 0 && !c.exact) ? c.pin[kBatchLS + b] : 0.0;
+    c.cand_xmin[b] = xmin[b];
+  }
 }
 
 // Projected backtracking line search: Lalpha_min_auglag (440-483) in the
@@ -1283,13 +1309,15 @@ static void line_search(Ctx& c, bool stage2, double& alpha, double& dlalpha) {
   alpha = ls.alphamin;
 }
 
-// Mixed path: the two FP64 slope probes (alpha = 0, dx) as in the
-// reference; the probes alpha = 1, 0.75, ... are screened with their
-// objective change relative to the alpha = 0 candidate X0,
+// Mixed path: the reference's probes (alpha = dx for the slope, then 1,
+// 0.75, ...) are evaluated as objective changes relative to the alpha = 0
+// candidate X0 (the iterate),
 //   L(X_a) - L(X0) = sum F.dX (2 r0 + F.dX) + Lgam(X_a) - Lgam(X0),
-// dX = X_a - X0 (projected), products in FP32 and sums in FP64; the chosen
-// step then gets an FP64 objective and sufficient-decrease check, and if it
-// fails the reference's FP64 sequence continues from the next probe.
+// dX = X_a - X0 (projected), products in FP32 and sums in FP64 (the change
+// itself to ~1e-6 relative, where a difference of FP32 objectives would be
+// off by ~1e-2); the chosen step then gets an FP64 objective and
+// sufficient-decrease check, and if it fails the reference's FP64 sequence
+// continues from the next probe.
 static void line_search_mixed(Ctx& c, bool stage2, double& alpha, double& dlalpha) {
   Scope s(c.timers, "Lalpha_min");
   const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
@@ -1302,22 +1330,9 @@ static void line_search_mixed(Ctx& c, bool stage2, double& alpha, double& dlalph
   CK(cudaMemcpyAsync(c.x0c.p, c.X.p, MN * sizeof(double), cudaMemcpyDeviceToDevice, c.st));
   k_half_to32<<<elem_grid(DN), 256, 0, c.st>>>(c.R.p, DN, 0.5f, c.r0_32.p);
   post_launch(c);
-  double al[1] = {0.0 + kDx}, L[1], xm[1];
-  eval_candidates(c, al, 1, stage2, L, xm);
-  LSState ls;
-  ls.L0 = L0;
-  ls.df = (L[0] - ls.L0) / kDx;
-  dlalpha = ls.df;
-  double qa[kBatchLS], xmin[kBatchLS], dres[kBatchLS], lg[kBatchLS];
   const int g = elem_grid(MN), g2 = elem_grid(DN);
-  bool screened_stop = false;
-  double stop_a = 0.0;  // alpha of the probe where the screened sequence stopped
-  while (!ls.done && ls.i <= kMaxLS) {
-    const int nb = std::min(kBatchLS, kMaxLS - ls.i + 1);
-    for (int k = 0; k < nb; ++k) {
-      qa[k] = ls.next_a;
-      ls.next_a = ls.next_a * 0.75;
-    }
+  // objective changes L(X_a) - L(X0) of nb projected probes -> dL[], xmin[]
+  auto screen = [&](const double* qa, int nb, double* dL, double* xmin) {
     CK(cudaMemcpyAsync(c.alphas.p, qa, nb * sizeof(double), cudaMemcpyHostToDevice, c.st));
     if (stage2) {
       const int gb = cdiv(M, kRowThreads);
@@ -1345,12 +1360,31 @@ static void line_search_mixed(Ctx& c, bool stage2, double& alpha, double& dlalph
     CK(cudaStreamSynchronize(c.st));
     for (int k = 0; k < nb; ++k) {
       xmin[k] = stage2 ? c.pin[2 * kBatchLS + k] : 0.0;
-      dres[k] = c.pin[3 * kBatchLS + k];
-      lg[k] = c.h.gam != 0 ? c.pin[kBatchLS + k] - Lgam0 : 0.0;
+      dL[k] = c.pin[3 * kBatchLS + k] + (c.h.gam != 0 ? c.pin[kBatchLS + k] - Lgam0 : 0.0);
     }
     c.n_lsL += nb;
+  };
+  // the slope probe alpha = dx (404, 450) as an objective change: a
+  // difference of two FP64 objectives ~1e-9 apart is what the reference
+  // divides by dx; here it is computed directly
+  double qa[kBatchLS], xmin[kBatchLS], dl[kBatchLS];
+  qa[0] = 0.0 + kDx;
+  screen(qa, 1, dl, xmin);
+  LSState ls;
+  ls.L0 = L0;
+  ls.df = dl[0] / kDx;
+  dlalpha = ls.df;
+  bool screened_stop = false;
+  double stop_a = 0.0;  // alpha of the probe where the screened sequence stopped
+  while (!ls.done && ls.i <= kMaxLS) {
+    const int nb = std::min(kBatchLS, kMaxLS - ls.i + 1);
+    for (int k = 0; k < nb; ++k) {
+      qa[k] = ls.next_a;
+      ls.next_a = ls.next_a * 0.75;
+    }
+    screen(qa, nb, dl, xmin);
     for (int k = 0; k < nb && !ls.done; ++k)
-      if (ls_take(c, ls, stage2, qa[k], ls.L0 + dres[k] + lg[k], xmin[k])) {
+      if (ls_take(c, ls, stage2, qa[k], ls.L0 + dl[k], xmin[k])) {
         screened_stop = true;
         stop_a = qa[k];
       }
@@ -1475,13 +1509,38 @@ static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
     if (c.precision == PQDTS_MIXED && !c.refine && !c.fullspace && (st.alpha == 0.0 || st.dlalpha >= 0.0))
       c.refine = true;
   }
-  if (st.alpha != 0.0) {
+  // Mixed path: the chosen step was evaluated in FP64 as a line-search
+  // candidate (projected, rebuilt, its residual and objective known): adopt
+  // it instead of recomputing the same projection and banded product.
+  int adopt = -1;
+  if (!c.exact && st.alpha != 0.0 && c.cand_xver == c.xver && c.cand_stage2 == !c.fullspace)
+    for (int b = 0; b < c.cand_B; ++b)
+      if (c.cand_alpha[b] == st.alpha) {
+        adopt = b;
+        break;
+      }
+  st.xmin = 0.0;
+  if (adopt >= 0) {
+    const int64_t DN = c.h.D * c.h.N;
+    CK(cudaMemcpyAsync(c.X.p, c.Xc.p + (size_t)adopt * MN, MN * sizeof(double), cudaMemcpyDeviceToDevice, c.st));
+    touch_x(c);
+    k_scale_copy<<<elem_grid(DN), 256, 0, c.st>>>(DN, 2.0, c.Rst.p + (size_t)adopt * DN, c.R.p);
+    post_launch(c);
+    c.R_ver = c.xver;
+    c.L_cache = c.cand_L[adopt];
+    c.Lgam_cache = c.cand_Lgam[adopt];
+    c.L_ver = c.xver;
+    if (!c.fullspace) {
+      c.rebuilt_ver = c.xver;
+      st.xmin = c.cand_xmin[adopt];
+    }
+  } else if (st.alpha != 0.0) {
     k_axpy<<<g, 256, 0, c.st>>>(MN, st.alpha, c.sn64.p, c.X.p);
     post_launch(c);
     touch_x(c);
   }
-  st.xmin = 0.0;
-  if (c.fullspace) {
+  if (adopt >= 0) {
+  } else if (c.fullspace) {
     Scope s(c.timers, "doproj");
     project_rows(c, c.X.p, nullptr, nullptr, c.X.p, 1);
     touch_x(c);
@@ -1721,24 +1780,50 @@ static void tune_schedule(Ctx& c, Schedule& s) {
   }
   if (c.precision != PQDTS_MIXED) return;
   if (s.tc) {
-    // tensor-core F^T product: K splits of at most 1 GiB of partials
+    // tensor-core products: N tile width x K splits of the F^T product
+    // (partials of at most 1 GiB)
     const int max_splits = (int)std::max<int64_t>(1, std::min<int64_t>(8, ((int64_t)1 << 30) / (MN * 4)));
     c.hpart32.alloc((size_t)std::max(max_splits, s.tc_splits) * MN);
+    CK(cudaMemsetAsync(c.vt_hi.p, 0, c.vt_hi.n * sizeof(__nv_bfloat16), c.st));
+    CK(cudaMemsetAsync(c.vt_lo.p, 0, c.vt_lo.n * sizeof(__nv_bfloat16), c.st));
     CK(cudaMemsetAsync(c.yt_hi.p, 0, c.yt_hi.n * sizeof(__nv_bfloat16), c.st));
     CK(cudaMemsetAsync(c.yt_lo.p, 0, c.yt_lo.n * sizeof(__nv_bfloat16), c.st));
+    auto fwd = [&] {
+      tc_product(c, c.tcF, c.map_vt_hi, c.map_vt_lo, D, 1, 1, 2.0f, nullptr, c.yt_hi.p, c.yt_lo.p, c.tc_dp, nullptr);
+    };
     auto trn = [&](int sp) {
       tc_product(c, c.tcFt, c.map_yt_hi, c.map_yt_lo, M, sp, 0, 1.0f, c.hpart32.p, nullptr, nullptr, 0, nullptr);
     };
-    float best = time_calls(c, kTuneReps, [&] { trn(s.tc_splits); });
-    if (best < kTuneMaxMs)
-      for (int sp : {1, 2, 3, 4, 6, 8}) {
-        if (sp > max_splits || sp == s.tc_splits) continue;
-        const float t = time_calls(c, kTuneReps, [&] { trn(sp); });
-        if (t < best * (sp > s.tc_splits ? 0.97f : 1.0f)) {
-          best = t;
-          s.tc_splits = sp;
+    float best = 0.0f;
+    int best_bn = s.tc_bn, best_sp = s.tc_splits;
+    bool first = true;
+    for (int mult : {1, 2, 4}) {
+      const int bn = tc_tile_n(N, mult);
+      if (!first && (bn == c.tc_bn || bn < 32)) continue;
+      tc_configure(c, bn);
+      const float t1 = time_calls(c, kTuneReps, fwd);
+      int sp_best = s.tc_splits;
+      float t2 = time_calls(c, kTuneReps, [&] { trn(sp_best); });
+      if (t1 + t2 < kTuneMaxMs)
+        for (int sp : {1, 2, 3, 4, 6, 8}) {
+          if (sp > max_splits || sp == s.tc_splits) continue;
+          const float t = time_calls(c, kTuneReps, [&] { trn(sp); });
+          if (t < t2 * (sp > sp_best ? 0.97f : 1.0f)) {
+            t2 = t;
+            sp_best = sp;
+          }
         }
+      if (first || t1 + t2 < best) {
+        best = t1 + t2;
+        best_bn = bn;
+        best_sp = sp_best;
       }
+      first = false;
+      if (t1 + t2 >= kTuneMaxMs) break;
+    }
+    tc_configure(c, best_bn);
+    s.tc_bn = best_bn;
+    s.tc_splits = best_sp;
     return;
   }
   CGBufs<float>& b = c.cg32;
@@ -1786,6 +1871,7 @@ static void choose_schedule(Ctx& c) {
   Schedule s = heuristic_schedule(h);
   if (c.tc_ready) {
     s.tc = 1;
+    s.tc_bn = c.tc_bn;
     const int64_t ctas = (int64_t)cdiv(h.N, c.tc_bn) * c.tcFt.blocks;
     s.tc_splits = (int)std::min<int64_t>(8, std::max<int64_t>(1, (152 + ctas - 1) / ctas));
   }
@@ -1797,6 +1883,7 @@ static void choose_schedule(Ctx& c) {
     auto it = g_sched.find(key);
     if (it != g_sched.end()) {
       s = it->second;
+      if (s.tc) tc_configure(c, s.tc_bn);
     } else {
       tune_schedule(c, s);
       s.tuned = 1;
@@ -2277,6 +2364,7 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     else if (n == "sched.tuned") *value = s.tuned;
     else if (n == "sched.tc") *value = s.tc;
     else if (n == "sched.tc_splits") *value = s.tc_splits;
+    else if (n == "sched.tc_bn") *value = s.tc_bn;
     else if (n == "tensor_cores") *value = c->tc_option;
     else if (n == "graphs.captured") *value = (int64_t)c->graphs.size();
     else throw pqdts::Err(PQDTS_E_ARG, "unknown option " + n);

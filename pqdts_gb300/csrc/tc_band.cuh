@@ -263,32 +263,59 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   if (!ok) s_abort = 1;
   const int r = r0 + warp * 32 + lane;
   const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-  for (int cc = 0; cc < BN; cc += 16) {
-    float v[16];
-    if (nk > 0) {
-      tc_ld16(trow + (uint32_t)cc, v);
-    } else {
+  // the warp's decision (uniform: the loads below are warp-collective)
+  const bool store = __all_sync(0xffffffffu, ok && !s_abort);
+  if (mode == 0) {
+    // FP32 rows: staged through the (now idle) stage ring so each store
+    // instruction writes 128 contiguous bytes of one row; warp w uses rows
+    // 32w..32w+31 of the tile, row stride = 1 mod 32 words (no bank conflicts)
+    const int stride = BN + ((33 - BN % 32) % 32);
+    float* mine = reinterpret_cast<float*>(base) + (size_t)(warp * 32) * stride;
+    for (int cc = 0; cc < BN; cc += 16) {
+      float v[16];
+      if (nk > 0) {
+        tc_ld16(trow + (uint32_t)cc, v);
+      } else {
 #pragma unroll
-      for (int j = 0; j < 16; ++j) v[j] = 0.f;
-    }
-    const bool store = !s_abort && r < R;  // (the loads above stay warp-converged)
-    if (!store) {
-    } else if (mode == 0) {
-      float* o = out + (int64_t)blockIdx.z * out_stride + (int64_t)r * N;
-#pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        const int n = n0 + cc + j;
-        if (n < N) o[n] = scale * v[j];
+        for (int j = 0; j < 16; ++j) v[j] = 0.f;
       }
-    } else {
+      if (store) {
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        const int n = n0 + cc + j;
-        if (n < N) {
-          const float x = scale * v[j];
-          const __nv_bfloat16 h = __float2bfloat16_rn(x);
-          oh[(int64_t)n * ld + r] = h;
-          ol[(int64_t)n * ld + r] = __float2bfloat16_rn(x - __bfloat162float(h));
+        for (int j = 0; j < 16; ++j) mine[lane * stride + cc + j] = v[j];
+      }
+    }
+    __syncwarp();
+    if (store) {
+      float* o = out + (int64_t)blockIdx.z * out_stride;
+      for (int rr = 0; rr < 32; ++rr) {
+        const int row = r0 + warp * 32 + rr;
+        if (row >= R) break;
+        for (int x = lane; x < BN; x += 32) {
+          const int n = n0 + x;
+          if (n < N) o[(int64_t)row * N + n] = scale * mine[rr * stride + x];
+        }
+      }
+    }
+  } else {
+    // (F.V)^T split: for each column n the warp writes 32 consecutive rows
+    for (int cc = 0; cc < BN; cc += 16) {
+      float v[16];
+      if (nk > 0) {
+        tc_ld16(trow + (uint32_t)cc, v);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = 0.f;
+      }
+      if (store && r < R) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int n = n0 + cc + j;
+          if (n < N) {
+            const float x = scale * v[j];
+            const __nv_bfloat16 h = __float2bfloat16_rn(x);
+            oh[(int64_t)n * ld + r] = h;
+            ol[(int64_t)n * ld + r] = __float2bfloat16_rn(x - __bfloat162float(h));
+          }
         }
       }
     }
