@@ -383,6 +383,8 @@ def run_ours(args):
     # time to an objective within 1e-8 relative of L64
     extra = {}
     if prec == pq.FP64 and args.with_mixed and world == 1:
+        X64 = s64.get_x()  # the FP64 solve's result (the last timed solve)
+
         def mixed_run(tc):
             with pq.Solver(local) as sm:
                 sm.set_option("tensor_cores", tc)
@@ -399,6 +401,7 @@ def run_ours(args):
                        "rel_obj_vs_L64": (ms[-1]["L"] - L64) / L64, "reached": ms[-1]["L"] <= target,
                        "outer": ms[-1]["outer"], "cg": ms[-1]["cg"], "refine": ms[-1]["refine"],
                        "tensor_cores": bool(sm.get_option("sched.tc")),
+                       "max_abs_pi_vs_fp64": float(np.max(np.abs(sm.get_x() - X64))),
                        "hessian_product_pair": {"us_per_cg_iteration": bft / cgs * 1e6 if cgs else None,
                                                 "algorithmic_tflops": flops_pair * cgs / bft / 1e12 if bft else None}}
                 return out
@@ -509,7 +512,9 @@ def run_workload(name, args):
                  the FP64 solves one after another for comparison);
       config3 -- M=10000, N=1000, D=20000: FP64 vs mixed (tensor-core and
                  CUDA-core Hessian products) over the first outer iterations;
-      dense   -- the same on the dense-F variant M=D=8192, N=256."""
+      dense   -- the same on the dense-F variant M=D=8192, N=256;
+      config5 -- the same at M=50000, N=5000, D=100000 (one outer
+                 iteration per stage by default)."""
     import numpy as np
 
     import pqdts_gb300 as pq
@@ -550,12 +555,16 @@ def run_workload(name, args):
             out["fp64"]["identical_objectives"] = bool(np.array_equal(np.array(Ls), L64))
         print(json.dumps(out))
         return 0
-    if name in ("config3", "dense"):
-        cfg = 3 if name == "config3" else 6
+    if name in ("config3", "dense", "config5"):
+        cfg = {"config3": 3, "dense": 6, "config5": 5}[name]
+        iters = args.config5_iters if cfg == 5 else args.config3_iters
+        t0 = time.perf_counter()
         inst = synth.make_config(cfg, seed=0)
-        out = {"workload": ("M=10000 N=1000 D=20000 (banded F)" if cfg == 3 else
-                            "M=8192 N=256 D=8192 (dense F, every entry kept)"), "nnz_F": inst.nnz,
-               "iterations": args.config3_iters}
+        gen_s = time.perf_counter() - t0
+        out = {"workload": {3: "M=10000 N=1000 D=20000 (banded F)",
+                            6: "M=8192 N=256 D=8192 (dense F, every entry kept)",
+                            5: "M=50000 N=5000 D=100000 (banded F)"}[cfg], "nnz_F": inst.nnz,
+               "iterations_per_stage": iters, "generation_s": gen_s}
         flops_pair = 2 * 2.0 * inst.nnz * inst.N
         for prec, tc, tag in ((pq.FP64, 0, "fp64"), (pq.MIXED, -1, "mixed_tc"), (pq.MIXED, 0, "mixed_cuda_cores")):
             with pq.Solver(0) as s:
@@ -563,7 +572,7 @@ def run_workload(name, args):
                 s.set_instance(inst, prec)
                 s.init_x()
                 t0 = time.perf_counter()
-                st = s.solve(mode=2, maxiter=args.config3_iters, eps=EPS)
+                st = s.solve(mode=2, maxiter=iters, eps=EPS)
                 el = time.perf_counter() - t0
                 bf = s.timer("BF")
                 out[tag] = {"seconds": el, "outer": st["outer"], "cg": st["cg"],
@@ -591,12 +600,13 @@ def main():
     ap.add_argument("--ref-sample-iters", type=int, default=3)
     ap.add_argument("--profile-case", choices=["fp64", "mixed", "solve64", "solvemix", "tc3", "tcdense"], default=None,
                     help="launches of the workload for ncu (see run_profile_case)")
-    ap.add_argument("--workload", choices=["batch", "config3", "dense"], default=None,
+    ap.add_argument("--workload", choices=["batch", "config3", "dense", "config5"], default=None,
                     help="secondary measurement instead of the bench line")
     ap.add_argument("--batch-maxiter", type=int, default=200)
     ap.add_argument("--batch-sequential", action="store_true",
                     help="batch workload: also time the FP64 solves one after another")
     ap.add_argument("--config3-iters", type=int, default=3)
+    ap.add_argument("--config5-iters", type=int, default=1)
     args = ap.parse_args()
     if args.workload:
         return run_workload(args.workload, args)
