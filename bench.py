@@ -457,12 +457,14 @@ def run_profile_case(case):
     import pqdts_gb300 as pq
     from pqdts_gb300 import synth
 
-    if case in ("tc3", "tcdense"):
+    if case in ("tc3", "tcdense", "tc3p", "tcdensep"):
         # the tensor-core Hessian product pair (3 BF32 calls, no autotuning
-        # launches) at M=10000 N=1000 D=20000, or on the dense-F variant
-        inst = synth.make_config(3 if case == "tc3" else 6, seed=0)
+        # launches) at M=10000 N=1000 D=20000, or on the dense-F variant;
+        # ...p: the persistent kernel
+        inst = synth.make_config(3 if case.startswith("tc3") else 6, seed=0)
         with pq.Solver(0) as s:
             s.set_option("autotune", 0)
+            s.set_option("tc_persistent", 1 if case.endswith("p") else 0)
             s.set_instance(inst, pq.MIXED)
             assert s.get_option("sched.tc") == 1
             rng = np.random.default_rng(0)
@@ -543,6 +545,7 @@ def run_workload(name, args):
                         "cg_total": sum(x["cg"] for x in stm), "max_rel_objective_vs_fp64": float(rel.max()),
                         "instances_at_target": int((Lm <= L64 * (1.0 + OBJ_REL)).sum())}
         out["mixed_speedup_vs_fp64"] = t64 / tmix
+        out["workers"] = int(os.environ.get("PQDTS_BATCH_WORKERS", "8"))
         if args.batch_sequential:
             # the same FP64 solves one after another through one context
             t0 = time.perf_counter()
@@ -598,7 +601,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-iters", type=int, default=4)
     ap.add_argument("--ref-sample-iters", type=int, default=3)
-    ap.add_argument("--profile-case", choices=["fp64", "mixed", "solve64", "solvemix", "tc3", "tcdense"], default=None,
+    ap.add_argument("--profile-case", choices=["fp64", "mixed", "solve64", "solvemix", "tc3", "tcdense", "tc3p",
+                                               "tcdensep"], default=None,
                     help="launches of the workload for ncu (see run_profile_case)")
     ap.add_argument("--workload", choices=["batch", "config3", "dense", "config5"], default=None,
                     help="secondary measurement instead of the bench line")

@@ -15,6 +15,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <map>
@@ -245,6 +246,7 @@ struct Schedule {
   int tc = 0;             // mixed CG products on the tensor cores (split-BF16x3)
   int tc_splits = 1;      // K segments of their F^T product
   int tc_bn = 0;          // their N tile width
+  int tc_persistent = 0;  // 1: persistent warp-specialized kernel, 0: one CTA per tile
 };
 
 // Band operand of the tensor-core products: 128-row blocks of bf16 hi/lo
@@ -290,6 +292,8 @@ struct pqdts_ctx {
   pqdts::DBuf<int64_t> foff, tptr;
   pqdts::DBuf<double> fval, tval, bdiag, P;
   pqdts::DBuf<float> fval32, tval32, tbval32, rsq32;
+  pqdts::DBuf<double> sqd;  // sqrt(bdfac * Bdiag) per row, FP64 CG step
+  pqdts::DBuf<unsigned> counters;  // grid-completion counters of fused reductions (kept at 0 between launches)
   pqdts::DBuf<int32_t> tlo, tw;
   pqdts::DBuf<int64_t> toff;
   // iterate and work arrays
@@ -337,6 +341,8 @@ struct pqdts_ctx {
   // tensor-core Hessian products of the mixed CG: option (-1 auto, 0 off,
   // 1 on), operands F and F^T, the split B operands V^T and (2 F.V)^T
   int tc_option = -1;
+  int tc_persistent_option = -1;  // -1 autotuned, 0 one CTA per tile, 1 persistent
+  int num_sms = 0;
   bool tc_ready = false;
   int tc_bn = 0, tc_stages = 0;
   int64_t tc_mp = 0, tc_dp = 0;  // row strides (elements) of V^T and (F.V)^T
@@ -441,6 +447,9 @@ static void setup_device(Ctx& c) {
     c.tbval32.release();
   }
   c.cg64.alloc(MN, M, D * N);
+  c.sqd.alloc(M);
+  c.counters.alloc(4);
+  CK(cudaMemsetAsync(c.counters.p, 0, 4 * sizeof(unsigned), c.st));
   c.exact = (c.precision == PQDTS_FP64);
   // residual stack of the line-search candidates (both precisions)
   c.Rst.alloc((size_t)kBatchLS * D * N);
@@ -857,6 +866,8 @@ static void setup_tc(Ctx& c) {
   c.yt_hi.alloc((size_t)N * c.tc_dp);
   c.yt_lo.alloc((size_t)N * c.tc_dp);
   CK(cudaFuncSetAttribute(k_tc_band, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcMaxSmem));
+  CK(cudaFuncSetAttribute(k_tc_band_p, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcMaxSmem));
+  CK(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, c.device));
   tc_configure(c, bn);
   c.tc_ready = true;
 }
@@ -866,13 +877,21 @@ static void setup_tc(Ctx& c) {
 // the K range, out_stride apart), mode 1: transposed bf16 split into oh / ol.
 static void tc_product(Ctx& c, const TcOperand& A, const CUtensorMap& bhi, const CUtensorMap& blo, int R, int splits,
                        int mode, float scale, float* out, __nv_bfloat16* oh, __nv_bfloat16* ol, int64_t ld,
-                       const double* pred) {
+                       const double* pred, int persistent) {
   const int N = (int)c.h.N;
-  const dim3 grid(cdiv(N, c.tc_bn), A.blocks, splits);
   const size_t smem = (size_t)c.tc_stages * tc_stage_bytes(c.tc_bn) + 1024;
-  k_tc_band<<<grid, kTcThreads, smem, c.st>>>(A.map_hi, A.map_lo, bhi, blo, A.kb.p, A.nch.p, R, N, c.tc_bn,
-                                              c.tc_stages, splits, mode, scale, out, (int64_t)R * N, oh, ol, ld, pred,
-                                              c.sc.p + SC_TCERR);
+  if (persistent) {
+    const int64_t tiles = (int64_t)cdiv(N, c.tc_bn) * A.blocks * splits;
+    const int grid = (int)std::min<int64_t>(tiles, c.num_sms);
+    k_tc_band_p<<<grid, kTcpThreads, smem, c.st>>>(A.map_hi, A.map_lo, bhi, blo, A.kb.p, A.nch.p, R, N, c.tc_bn,
+                                                   c.tc_stages, splits, A.blocks, mode, scale, out, (int64_t)R * N, oh,
+                                                   ol, ld, pred, c.sc.p + SC_TCERR);
+  } else {
+    const dim3 grid(cdiv(N, c.tc_bn), A.blocks, splits);
+    k_tc_band<<<grid, kTcThreads, smem, c.st>>>(A.map_hi, A.map_lo, bhi, blo, A.kb.p, A.nch.p, R, N, c.tc_bn,
+                                                c.tc_stages, splits, mode, scale, out, (int64_t)R * N, oh, ol, ld, pred,
+                                                c.sc.p + SC_TCERR);
+  }
   post_launch(c);
 }
 
@@ -883,9 +902,10 @@ static void tc_hvp_products(Ctx& c, const float* src, const double* pred) {
   const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
   k_split_t<<<dim3(cdiv(M, 32), cdiv(N, 32)), dim3(32, 8), 0, c.st>>>(src, M, N, c.tc_mp, c.vt_hi.p, c.vt_lo.p, pred);
   post_launch(c);
-  tc_product(c, c.tcF, c.map_vt_hi, c.map_vt_lo, D, 1, 1, 2.0f, nullptr, c.yt_hi.p, c.yt_lo.p, c.tc_dp, pred);
+  tc_product(c, c.tcF, c.map_vt_hi, c.map_vt_lo, D, 1, 1, 2.0f, nullptr, c.yt_hi.p, c.yt_lo.p, c.tc_dp, pred,
+             c.sched.tc_persistent);
   tc_product(c, c.tcFt, c.map_yt_hi, c.map_yt_lo, M, c.sched.tc_splits, 0, 1.0f, c.hpart32.p, nullptr, nullptr, 0,
-             pred);
+             pred, c.sched.tc_persistent);
 }
 
 // Out (R x N) = scale * Band (R rows) . In with tile code `tile` (0 = 64x64,
@@ -950,11 +970,11 @@ static void hvp32(Ctx& c, CGBufs<float>& b, const int8_t* ik, bool with_dot, con
                        pred, parts, 0, (int64_t)M * N, parts);
   }
   const int tb = std::min(256, std::max(32, cdiv(N, 32) * 32));
+  // p.Hp -> sc[SC_V2] by the epilogue's last row block
   k_hvp_epi32<<<M, tb, 0, c.st>>>(c.hpart32.p, b.p.p, c.fullspace ? nullptr : b.rs.p, c.maxr.p, c.fullspace ? 0 : 1,
                                   (float)(2.0 * c.h.gam), ik, M, N, b.Hp.p, with_dot ? c.part.p : nullptr, pred,
-                                  parts);
+                                  parts, with_dot ? c.sc.p + SC_V2 : nullptr, c.counters.p);
   post_launch(c);
-  if (with_dot) reduce_to(c, c.part.p, M, c.sc.p + SC_V2, 1, false, 0.0, pred);
 }
 
 // A chunk of CG iterations captured as a CUDA graph (on first use of its
@@ -1074,12 +1094,9 @@ static void cg_solve32(Ctx& c, double bdfac) {
       Scope sb(c.timers, "BF");
       hvp32(c, b, c.ik.p, true, c.sc.p);
     }
+    // the step; its last block sums r.z, r.r and advances the CG scalars
     k_cg_step32<<<g, 256, 0, c.st>>>(c.sc.p, c.rsq32.p, M, N, b.p.p, b.Hp.p, b.sn.p, b.r.p, b.z.p, c.part.p,
-                                     c.part2.p);
-    post_launch(c);
-    reduce_to(c, c.part.p, g, c.sc.p + SC_RZ, 1, false, 0.0, c.sc.p);
-    reduce_to(c, c.part2.p, g, c.sc.p + SC_RR, 1, false, 0.0, c.sc.p);
-    k_cg_scalars1<<<1, 1, 0, c.st>>>(c.sc.p, c.cglog.p, kMaxCG);
+                                     c.part2.p, c.cglog.p, kMaxCG, c.counters.p + 1);
     post_launch(c);
   };
   const int done_iters = cg_chunks(c, {0, (uint64_t)c.fullspace, 0, 0}, iteration);
@@ -1110,6 +1127,8 @@ static void cg_solve(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, double bdfa
   Scope s(c.timers, "CG");
   k_cg_init<T><<<g, 256, 0, c.st>>>(c.X.p, c.G.p, c.bdiag.p, bdfac, kActiveTol, M, N, c.ik.p, b.r.p, b.z.p, b.p.p,
                                     b.sn.p, c.part.p, c.part2.p, c.ipart.p);
+  post_launch(c);
+  k_sqrt_diag<<<cdiv(M, 256), 256, 0, c.st>>>(c.bdiag.p, bdfac, M, c.sqd.p);
   post_launch(c);
   constexpr bool kF64 = std::is_same<T, double>::value;
   const bool exact = kF64 && c.exact;
@@ -1156,7 +1175,7 @@ static void cg_solve(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, double bdfa
     }
     if constexpr (kF64)
       if (exact) dot_dev(c, b.p.p, b.Hp.p, c.sc.p + SC_V2, c.sc.p);
-    k_cg_step<T><<<g, 256, 0, c.st>>>(c.sc.p, c.bdiag.p, bdfac, M, N, b.p.p, b.Hp.p, b.sn.p, b.r.p, b.z.p, c.part.p,
+    k_cg_step<T><<<g, 256, 0, c.st>>>(c.sc.p, c.sqd.p, M, N, b.p.p, b.Hp.p, b.sn.p, b.r.p, b.z.p, c.part.p,
                                       c.part2.p);
     post_launch(c);
     if (exact) {
@@ -1689,7 +1708,7 @@ static void solve(Ctx& c, int mode, int maxiiter, double conv_thres, int start_s
 // one bucket (a resampled or gamma-swept batch) are tuned once.
 // ---------------------------------------------------------------------------
 static std::mutex g_sched_mu;
-static std::map<std::array<int64_t, 7>, Schedule> g_sched;
+static std::map<std::array<int64_t, 8>, Schedule> g_sched;
 
 static int ilog2_ceil(int64_t v) {
   int k = 0;
@@ -1788,39 +1807,49 @@ static void tune_schedule(Ctx& c, Schedule& s) {
     CK(cudaMemsetAsync(c.vt_lo.p, 0, c.vt_lo.n * sizeof(__nv_bfloat16), c.st));
     CK(cudaMemsetAsync(c.yt_hi.p, 0, c.yt_hi.n * sizeof(__nv_bfloat16), c.st));
     CK(cudaMemsetAsync(c.yt_lo.p, 0, c.yt_lo.n * sizeof(__nv_bfloat16), c.st));
+    int pers = 0;
     auto fwd = [&] {
-      tc_product(c, c.tcF, c.map_vt_hi, c.map_vt_lo, D, 1, 1, 2.0f, nullptr, c.yt_hi.p, c.yt_lo.p, c.tc_dp, nullptr);
+      tc_product(c, c.tcF, c.map_vt_hi, c.map_vt_lo, D, 1, 1, 2.0f, nullptr, c.yt_hi.p, c.yt_lo.p, c.tc_dp, nullptr,
+                 pers);
     };
     auto trn = [&](int sp) {
-      tc_product(c, c.tcFt, c.map_yt_hi, c.map_yt_lo, M, sp, 0, 1.0f, c.hpart32.p, nullptr, nullptr, 0, nullptr);
+      tc_product(c, c.tcFt, c.map_yt_hi, c.map_yt_lo, M, sp, 0, 1.0f, c.hpart32.p, nullptr, nullptr, 0, nullptr,
+                 pers);
     };
     float best = 0.0f;
-    int best_bn = s.tc_bn, best_sp = s.tc_splits;
-    bool first = true;
+    int best_bn = s.tc_bn, best_sp = s.tc_splits, best_pers = s.tc_persistent;
+    bool first = true, large = false;
     for (int mult : {1, 2, 4}) {
       const int bn = tc_tile_n(N, mult);
       if (!first && (bn == c.tc_bn || bn < 32)) continue;
       tc_configure(c, bn);
-      const float t1 = time_calls(c, kTuneReps, fwd);
-      int sp_best = s.tc_splits;
-      float t2 = time_calls(c, kTuneReps, [&] { trn(sp_best); });
-      if (t1 + t2 < kTuneMaxMs)
-        for (int sp : {1, 2, 3, 4, 6, 8}) {
-          if (sp > max_splits || sp == s.tc_splits) continue;
-          const float t = time_calls(c, kTuneReps, [&] { trn(sp); });
-          if (t < t2 * (sp > sp_best ? 0.97f : 1.0f)) {
-            t2 = t;
-            sp_best = sp;
+      for (int pv : {0, 1}) {
+        if (c.tc_persistent_option >= 0 && pv != c.tc_persistent_option) continue;
+        pers = pv;
+        const float t1 = time_calls(c, kTuneReps, fwd);
+        int sp_best = s.tc_splits;
+        float t2 = time_calls(c, kTuneReps, [&] { trn(sp_best); });
+        if (t1 + t2 < kTuneMaxMs)
+          for (int sp : {1, 2, 3, 4, 6, 8}) {
+            if (sp > max_splits || sp == s.tc_splits) continue;
+            const float t = time_calls(c, kTuneReps, [&] { trn(sp); });
+            if (t < t2 * (sp > sp_best ? 0.97f : 1.0f)) {
+              t2 = t;
+              sp_best = sp;
+            }
           }
+        if (first || t1 + t2 < best) {
+          best = t1 + t2;
+          best_bn = bn;
+          best_sp = sp_best;
+          best_pers = pv;
         }
-      if (first || t1 + t2 < best) {
-        best = t1 + t2;
-        best_bn = bn;
-        best_sp = sp_best;
+        first = false;
+        if (t1 + t2 >= kTuneMaxMs) large = true;
       }
-      first = false;
-      if (t1 + t2 >= kTuneMaxMs) break;
+      if (large) break;
     }
+    s.tc_persistent = best_pers;
     tc_configure(c, best_bn);
     s.tc_bn = best_bn;
     s.tc_splits = best_sp;
@@ -1872,13 +1901,15 @@ static void choose_schedule(Ctx& c) {
   if (c.tc_ready) {
     s.tc = 1;
     s.tc_bn = c.tc_bn;
+    s.tc_persistent = c.tc_persistent_option == 1 ? 1 : 0;
     const int64_t ctas = (int64_t)cdiv(h.N, c.tc_bn) * c.tcFt.blocks;
     s.tc_splits = (int)std::min<int64_t>(8, std::max<int64_t>(1, (152 + ctas - 1) / ctas));
   }
   if (c.autotune) {
     const int64_t wavg = h.D > 0 ? std::max<int64_t>(1, h.nnz() / h.D) : 1;
-    const std::array<int64_t, 7> key{c.device,          c.precision,       h.N, ilog2_ceil(h.M), ilog2_ceil(h.D),
-                                     ilog2_ceil(wavg), (int64_t)s.tc};
+    const std::array<int64_t, 8> key{c.device,        c.precision,      h.N,
+                                     ilog2_ceil(h.M),  ilog2_ceil(h.D),  ilog2_ceil(wavg),
+                                     (int64_t)s.tc,    (int64_t)c.tc_persistent_option};
     std::lock_guard<std::mutex> lk(g_sched_mu);
     auto it = g_sched.find(key);
     if (it != g_sched.end()) {
@@ -2340,6 +2371,9 @@ int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
       c->use_graphs = value != 0;
     } else if (n == "autotune") {
       c->autotune = value != 0;
+    } else if (n == "tc_persistent") {
+      if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "tc_persistent must be -1, 0 or 1");
+      c->tc_persistent_option = (int)value;
     } else if (n == "tensor_cores") {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "tensor_cores must be -1, 0 or 1");
       c->tc_option = (int)value;
@@ -2365,6 +2399,8 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     else if (n == "sched.tc") *value = s.tc;
     else if (n == "sched.tc_splits") *value = s.tc_splits;
     else if (n == "sched.tc_bn") *value = s.tc_bn;
+    else if (n == "sched.tc_persistent") *value = s.tc_persistent;
+    else if (n == "tc_persistent") *value = c->tc_persistent_option;
     else if (n == "tensor_cores") *value = c->tc_option;
     else if (n == "graphs.captured") *value = (int64_t)c->graphs.size();
     else throw pqdts::Err(PQDTS_E_ARG, "unknown option " + n);
@@ -2398,7 +2434,10 @@ int pqdts_cuda_solve_batch(int32_t device, int32_t n_inst, const int64_t* M, con
   // context and stream, so the instances' kernels overlap on the device.
   std::vector<int64_t> xoff(n_inst + 1, 0);
   for (int k = 0; k < n_inst; ++k) xoff[k + 1] = xoff[k] + M[k] * N[k];
-  const int workers = std::min<int>(n_inst, 8);
+  // workers: PQDTS_BATCH_WORKERS (default 8), at most one per instance
+  int workers = 8;
+  if (const char* e = std::getenv("PQDTS_BATCH_WORKERS")) workers = std::max(1, std::min(64, std::atoi(e)));
+  workers = std::min<int>(n_inst, workers);
   std::atomic<int> next{0};
   std::atomic<int> rc{PQDTS_OK};
   std::mutex err_mu;

@@ -336,6 +336,214 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Persistent form of k_tc_band (same operands, modes and results): one CTA
+// per SM walks the output tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...
+// (N tiles fastest, then row blocks, then K splits).  Six warps: warp 0
+// lane 0 issues the TMA loads, warp 1 lane 0 the MMAs (warp 1 owns the
+// tensor memory), warps 2-5 run the epilogue.  Two FP32 accumulators in
+// tensor memory let the epilogue of tile j overlap the MMAs of tile j+1,
+// and the shared-memory stage ring runs on across tiles.
+constexpr int kTcpThreads = 192;
+
+__global__ void __launch_bounds__(kTcpThreads, 1)
+    k_tc_band_p(const __grid_constant__ CUtensorMap mA_hi, const __grid_constant__ CUtensorMap mA_lo,
+                const __grid_constant__ CUtensorMap mB_hi, const __grid_constant__ CUtensorMap mB_lo,
+                const int32_t* __restrict__ blk_kb, const int32_t* __restrict__ blk_nch, int R, int N, int BN,
+                int stages, int splits, int blocks, int mode, float scale, float* __restrict__ out,
+                int64_t out_stride, __nv_bfloat16* __restrict__ oh, __nv_bfloat16* __restrict__ ol, int64_t ld,
+                const double* __restrict__ pred, double* __restrict__ err) {
+  if (pred != nullptr && pred[6] != 0.0) return;  // CG already converged
+  extern __shared__ uint8_t tc_smem_raw[];
+  __shared__ uint64_t bar_full[kTcMaxStages], bar_empty[kTcMaxStages], bar_tfull[2], bar_tempty[2];
+  __shared__ uint32_t s_tmem;
+  __shared__ volatile int s_abort;
+  __shared__ int s_issued, s_consumed;
+  __shared__ float s_stage[4][32][17];  // epilogue staging of mode 0, one 32 x 16 slab per warp
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntn = (N + BN - 1) / BN;
+  const int T = ntn * blocks * splits;
+  const uint32_t raw = smem_u32(tc_smem_raw);
+  uint8_t* base = tc_smem_raw + ((1024u - (raw & 1023u)) & 1023u);
+  const uint32_t a_bytes = kTcRows * 128u, b_bytes = (uint32_t)BN * 128u;
+  const uint32_t stage_bytes = 2u * a_bytes + 2u * b_bytes;
+  const uint32_t ncols = tc_tmem_cols(BN);  // per accumulator
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < stages; ++i) {
+      mbar_init(&bar_full[i], 1);
+      mbar_init(&bar_empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&bar_tfull[i], 1);
+      mbar_init(&bar_tempty[i], 128);
+    }
+    s_abort = 0;
+    s_issued = 0;
+    s_consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    tc_alloc(&s_tmem, 2 * ncols);
+    tc_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = s_tmem;
+
+  // tile t -> N tile, row block, K chunk range [c0, c1), block K start kb
+  auto tile = [&](int t, int& nt, int& blk, int& c0, int& c1, int& kb) {
+    nt = t % ntn;
+    const int rest = t / ntn;
+    blk = rest % blocks;
+    const int sp = rest / blocks;
+    kb = blk_kb[blk];
+    c0 = 0;
+    c1 = kb >= 0 ? blk_nch[blk] : 0;
+    if (splits > 1) {
+      const int per = (c1 + splits - 1) / splits;
+      c0 = min(c1, sp * per);
+      c1 = min(c1, c0 + per);
+    }
+  };
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int it = 0;
+      for (int t = blockIdx.x; t < T && !s_abort; t += gridDim.x) {
+        int nt, blk, c0, c1, kb;
+        tile(t, nt, blk, c0, c1, kb);
+        for (int ch = c0; ch < c1 && !s_abort; ++ch, ++it) {
+          const int st = it % stages;
+          const uint32_t ph = (uint32_t)(it / stages) & 1u;
+          if (!mbar_wait(&bar_empty[st], ph ^ 1u)) {
+            s_abort = 1;
+            break;
+          }
+          uint8_t* sa = base + (size_t)st * stage_bytes;
+          uint8_t* sb = sa + 2 * a_bytes;
+          mbar_expect_tx(&bar_full[st], stage_bytes);
+          const int kx = ch * kTcK;
+          tma_load_2d(sa, &mA_hi, kx, blk * kTcRows, &bar_full[st]);
+          tma_load_2d(sa + a_bytes, &mA_lo, kx, blk * kTcRows, &bar_full[st]);
+          tma_load_2d(sb, &mB_hi, kb + kx, nt * BN, &bar_full[st]);
+          tma_load_2d(sb + b_bytes, &mB_lo, kb + kx, nt * BN, &bar_full[st]);
+          s_issued = it + 1;
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = tc_idesc_bf16(kTcRows, BN);
+      int it = 0, j = 0;
+      for (int t = blockIdx.x; t < T && !s_abort; t += gridDim.x, ++j) {
+        int nt, blk, c0, c1, kb;
+        tile(t, nt, blk, c0, c1, kb);
+        const int buf = j & 1;
+        const uint32_t acc = tmem + (uint32_t)buf * ncols;
+        if (!mbar_wait(&bar_tempty[buf], ((uint32_t)(j >> 1) & 1u) ^ 1u)) {  // accumulator free
+          s_abort = 1;
+          break;
+        }
+        tc_fence_after();
+        for (int ch = c0; ch < c1; ++ch, ++it) {
+          const int st = it % stages;
+          const uint32_t ph = (uint32_t)(it / stages) & 1u;
+          if (!mbar_wait(&bar_full[st], ph)) {
+            s_abort = 1;
+            break;
+          }
+          s_consumed = it + 1;
+          tc_fence_after();
+          const uint32_t a_hi = smem_u32(base + (size_t)st * stage_bytes);
+          const uint32_t a_lo = a_hi + a_bytes, b_hi = a_hi + 2 * a_bytes, b_lo = b_hi + b_bytes;
+#pragma unroll
+          for (int k = 0; k < kTcK / 16; ++k) {
+            const uint32_t o = 32u * k;
+            tc_mma(acc, sw128_desc(a_lo + o), sw128_desc(b_hi + o), idesc, (ch > c0 || k > 0) ? 1u : 0u);
+            tc_mma(acc, sw128_desc(a_hi + o), sw128_desc(b_lo + o), idesc, 1u);
+            tc_mma(acc, sw128_desc(a_hi + o), sw128_desc(b_hi + o), idesc, 1u);
+          }
+          tc_commit(&bar_empty[st]);
+        }
+        tc_commit(&bar_tfull[buf]);  // (also with no MMAs: the epilogue then stores zeros)
+      }
+    }
+  } else {
+    // epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. + 31 = tile rows
+    const int q = warp & 3, ew = warp - 2;
+    int j = 0;
+    for (int t = blockIdx.x; t < T; t += gridDim.x, ++j) {
+      int nt, blk, c0, c1, kb;
+      tile(t, nt, blk, c0, c1, kb);
+      const int nk = c1 - c0, buf = j & 1;
+      const bool ok = mbar_wait(&bar_tfull[buf], (uint32_t)(j >> 1) & 1u);
+      tc_fence_after();
+      const bool store = __all_sync(0xffffffffu, ok && !s_abort);
+      if (!store) {
+        s_abort = 1;
+        break;
+      }
+      const uint32_t tacc = tmem + (uint32_t)buf * ncols + ((uint32_t)(q * 32) << 16);
+      const int n0 = nt * BN, rt = blk * kTcRows + q * 32, r = rt + lane;
+      for (int cc = 0; cc < BN; cc += 16) {
+        float v[16];
+        if (nk > 0) {
+          tc_ld16(tacc + (uint32_t)cc, v);
+        } else {
+#pragma unroll
+          for (int jj = 0; jj < 16; ++jj) v[jj] = 0.f;
+        }
+        if (mode == 0) {
+#pragma unroll
+          for (int jj = 0; jj < 16; ++jj) s_stage[ew][lane][jj] = v[jj];
+          __syncwarp();
+          float* o = out + (int64_t)(t / (ntn * blocks)) * out_stride;
+          const int col = lane & 15, n = n0 + cc + col;
+#pragma unroll 4
+          for (int rr = 0; rr < 32; rr += 2) {
+            const int row = rr + (lane >> 4);
+            if (rt + row < R && n < N) o[(int64_t)(rt + row) * N + n] = scale * s_stage[ew][row][col];
+          }
+          __syncwarp();
+        } else if (r < R) {
+#pragma unroll
+          for (int jj = 0; jj < 16; ++jj) {
+            const int n = n0 + cc + jj;
+            if (n < N) {
+              const float x = scale * v[jj];
+              const __nv_bfloat16 h = __float2bfloat16_rn(x);
+              oh[(int64_t)n * ld + r] = h;
+              ol[(int64_t)n * ld + r] = __float2bfloat16_rn(x - __bfloat162float(h));
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&bar_tempty[buf]);  // accumulator read out
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (s_abort && threadIdx.x == 0) {
+    *err = 1.0;
+    for (int it = s_consumed; it < s_issued; ++it)
+      if (!mbar_wait(&bar_full[it % stages], (uint32_t)(it / stages) & 1u)) break;
+  }
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tc_dealloc(tmem, 2 * ncols);
+  }
+}
+
 // V (M x N row-major FP32) -> V^T split: hi[n * ld + i], lo[n * ld + i].
 __global__ void k_split_t(const float* __restrict__ V, int M, int N, int64_t ld, __nv_bfloat16* __restrict__ hi,
                           __nv_bfloat16* __restrict__ lo, const double* __restrict__ pred) {

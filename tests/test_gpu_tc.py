@@ -13,13 +13,16 @@ pytestmark = pytest.mark.gpu
 TC_REL = 1e-4
 
 
-def _tc_solver(inst):
+def _tc_solver(inst, persistent=-1):
     import pqdts_gb300 as pq
 
     s = pq.Solver(0)
     s.set_option("tensor_cores", 1)
+    s.set_option("tc_persistent", persistent)
     s.set_instance(inst, pq.MIXED)
     assert s.get_option("sched.tc") == 1
+    if persistent >= 0:
+        assert s.get_option("sched.tc_persistent") == persistent
     return s
 
 
@@ -46,11 +49,14 @@ def tc_insts():
 
 @pytest.mark.parametrize("which", ["tiny", "cfg1", "medium", "dense"])
 @pytest.mark.parametrize("full", [True, False])
-def test_tc_hessian_product_matches_fp64(built, tc_insts, which, full):
+@pytest.mark.parametrize("persistent", [0, 1])
+def test_tc_hessian_product_matches_fp64(built, tc_insts, which, full, persistent):
+    """Both kernels: one CTA per output tile, and the persistent
+    warp-specialized one with double-buffered accumulators."""
     from oracle.oracle import Oracle
 
     inst = tc_insts[which]
-    s = _tc_solver(inst)
+    s = _tc_solver(inst, persistent)
     o = Oracle.from_instance(inst)
     rng = np.random.default_rng(11)
     X = rng.random((inst.M, inst.N))
@@ -66,7 +72,8 @@ def test_tc_hessian_product_matches_fp64(built, tc_insts, which, full):
     s.close()
 
 
-def test_tc_mixed_solve_reaches_fp64_objective(built, tc_insts):
+@pytest.mark.parametrize("persistent", [0, 1])
+def test_tc_mixed_solve_reaches_fp64_objective(built, tc_insts, persistent):
     """The mixed solve with tensor-core CG products ends within 1e-8 of the
     FP64 solve's objective (conv < 1e-9 pins it), feasible."""
     import pqdts_gb300 as pq
@@ -75,7 +82,7 @@ def test_tc_mixed_solve_reaches_fp64_objective(built, tc_insts):
     with pq.Solver(0) as s64:
         s64.set_instance(inst, pq.FP64)
         st64 = s64.solve(mode=2, maxiter=2000, eps=1e-9)
-    s = _tc_solver(inst)
+    s = _tc_solver(inst, persistent)
     st = s.solve(mode=2, maxiter=2000, eps=1e-9)
     X = s.get_x()
     s.close()
