@@ -59,6 +59,10 @@ int pqdts_cuda_kernel_launches(pqdts_ctx* ctx, int64_t* count);
  *              run on the tensor cores (tcgen05, split-BF16x3, FP32
  *              accumulation) on compute capability 10.x devices; 0: FP32
  *              CUDA-core tiles.  Takes effect at the next set_problem.
+ *   "tc_persistent" -1 (default, autotuned) / 0 / 1: the tensor-core kernel
+ *              form (one CTA per output tile, or persistent with
+ *              double-buffered accumulators); "tc_splits1" -1 (autotuned) or
+ *              1..8: K segments of the tensor-core F.V product.
  * Unknown names return PQDTS_E_ARG. */
 int pqdts_cuda_set_option(pqdts_ctx* ctx, const char* name, int64_t value);
 /* Reads an option above or a field of the schedule in use:
@@ -67,8 +71,9 @@ int pqdts_cuda_set_option(pqdts_ctx* ctx, const char* name, int64_t value);
  * "sched.trans_threads", "sched.trans_cols" (FP64 F^T product block shape),
  * "sched.tuned" (1 = timed, 0 = heuristic), "sched.tc" (1 = tensor-core
  * Hessian products in use), "sched.tc_bn" (their N tile width),
- * "sched.tc_splits" (K segments of their F^T product), "graphs.captured"
- * (graphs held). */
+ * "sched.tc_splits" (K segments of their F^T product), "sched.tc_splits1"
+ * (of their F.V product), "sched.tc_persistent" (kernel form),
+ * "graphs.captured" (graphs held). */
 int pqdts_cuda_get_option(pqdts_ctx* ctx, const char* name, int64_t* value);
 /* verbose = 1 prints the reference's stdout lines (iter, newton-pcg, line
  * search, positivity constraints) exactly as rank 0 of pqdts_omp.x. */

@@ -247,6 +247,7 @@ struct Schedule {
   int tc_splits = 1;      // K segments of their F^T product
   int tc_bn = 0;          // their N tile width
   int tc_persistent = 0;  // 1: persistent warp-specialized kernel, 0: one CTA per tile
+  int tc_splits1 = 1;     // K segments of their F.V product (> 1: FP32 partials + k_finish_t)
 };
 
 // Band operand of the tensor-core products: 128-row blocks of bf16 hi/lo
@@ -342,12 +343,14 @@ struct pqdts_ctx {
   // 1 on), operands F and F^T, the split B operands V^T and (2 F.V)^T
   int tc_option = -1;
   int tc_persistent_option = -1;  // -1 autotuned, 0 one CTA per tile, 1 persistent
+  int tc_splits1_option = -1;     // -1 autotuned, else the K segments of the tensor-core F.V product
   int num_sms = 0;
   bool tc_ready = false;
   int tc_bn = 0, tc_stages = 0;
   int64_t tc_mp = 0, tc_dp = 0;  // row strides (elements) of V^T and (F.V)^T
   pqdts::TcOperand tcF, tcFt;
   pqdts::DBuf<__nv_bfloat16> vt_hi, vt_lo, yt_hi, yt_lo;
+  pqdts::DBuf<float> ypart;  // FP32 partials of F.V when its K range is split
   CUtensorMap map_vt_hi, map_vt_lo, map_yt_hi, map_yt_lo;
   pqdts::Schedule sched;
   void drop_graphs() noexcept {
@@ -895,6 +898,23 @@ static void tc_product(Ctx& c, const TcOperand& A, const CUtensorMap& bhi, const
   post_launch(c);
 }
 
+// F.V on the tensor cores into the (2 F.V)^T split operand: directly from
+// the epilogue, or (splits1 > 1) through FP32 partials of its K segments.
+static void tc_forward(Ctx& c, int splits1, int persistent, const double* pred) {
+  const int N = (int)c.h.N, D = (int)c.h.D;
+  if (splits1 <= 1) {
+    tc_product(c, c.tcF, c.map_vt_hi, c.map_vt_lo, D, 1, 1, 2.0f, nullptr, c.yt_hi.p, c.yt_lo.p, c.tc_dp, pred,
+               persistent);
+    return;
+  }
+  require(c.ypart.p, "F.V partials");
+  tc_product(c, c.tcF, c.map_vt_hi, c.map_vt_lo, D, splits1, 0, 2.0f, c.ypart.p, nullptr, nullptr, 0, pred,
+             persistent);
+  k_finish_t<<<dim3(cdiv(D, 32), cdiv(N, 32)), dim3(32, 8), 0, c.st>>>(c.ypart.p, splits1, D, N, c.tc_dp, c.yt_hi.p,
+                                                                       c.yt_lo.p, pred);
+  post_launch(c);
+}
+
 // The Hessian product pair on the tensor cores: V -> V^T split, then
 // (2 F.V)^T split (written by the first product's epilogue), then the
 // partials of F^T.(2 F.V) in hpart32 (tc_splits of them).
@@ -902,8 +922,7 @@ static void tc_hvp_products(Ctx& c, const float* src, const double* pred) {
   const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
   k_split_t<<<dim3(cdiv(M, 32), cdiv(N, 32)), dim3(32, 8), 0, c.st>>>(src, M, N, c.tc_mp, c.vt_hi.p, c.vt_lo.p, pred);
   post_launch(c);
-  tc_product(c, c.tcF, c.map_vt_hi, c.map_vt_lo, D, 1, 1, 2.0f, nullptr, c.yt_hi.p, c.yt_lo.p, c.tc_dp, pred,
-             c.sched.tc_persistent);
+  tc_forward(c, c.sched.tc_splits1, c.sched.tc_persistent, pred);
   tc_product(c, c.tcFt, c.map_yt_hi, c.map_yt_lo, M, c.sched.tc_splits, 0, 1.0f, c.hpart32.p, nullptr, nullptr, 0,
              pred, c.sched.tc_persistent);
 }
@@ -1395,8 +1414,10 @@ static void line_search_mixed(Ctx& c, bool stage2, double& alpha, double& dlalph
   dlalpha = ls.df;
   bool screened_stop = false;
   double stop_a = 0.0;  // alpha of the probe where the screened sequence stopped
+  int batch = 2;        // probes per screening batch: 2 (the full step is usually taken), then 8
   while (!ls.done && ls.i <= kMaxLS) {
-    const int nb = std::min(kBatchLS, kMaxLS - ls.i + 1);
+    const int nb = std::min(batch, kMaxLS - ls.i + 1);
+    batch = kBatchLS;
     for (int k = 0; k < nb; ++k) {
       qa[k] = ls.next_a;
       ls.next_a = ls.next_a * 0.75;
@@ -1807,17 +1828,17 @@ static void tune_schedule(Ctx& c, Schedule& s) {
     CK(cudaMemsetAsync(c.vt_lo.p, 0, c.vt_lo.n * sizeof(__nv_bfloat16), c.st));
     CK(cudaMemsetAsync(c.yt_hi.p, 0, c.yt_hi.n * sizeof(__nv_bfloat16), c.st));
     CK(cudaMemsetAsync(c.yt_lo.p, 0, c.yt_lo.n * sizeof(__nv_bfloat16), c.st));
-    int pers = 0;
-    auto fwd = [&] {
-      tc_product(c, c.tcF, c.map_vt_hi, c.map_vt_lo, D, 1, 1, 2.0f, nullptr, c.yt_hi.p, c.yt_lo.p, c.tc_dp, nullptr,
-                 pers);
-    };
+    int pers = 0, sp1 = 1;
+    const int64_t DN = (int64_t)D * N;
+    const int max_splits1 = (int)std::max<int64_t>(1, std::min<int64_t>(4, ((int64_t)1 << 30) / (DN * 4)));
+    if (max_splits1 > 1) c.ypart.alloc((size_t)max_splits1 * DN);
+    auto fwd = [&] { tc_forward(c, sp1, pers, nullptr); };
     auto trn = [&](int sp) {
       tc_product(c, c.tcFt, c.map_yt_hi, c.map_yt_lo, M, sp, 0, 1.0f, c.hpart32.p, nullptr, nullptr, 0, nullptr,
                  pers);
     };
     float best = 0.0f;
-    int best_bn = s.tc_bn, best_sp = s.tc_splits, best_pers = s.tc_persistent;
+    int best_bn = s.tc_bn, best_sp = s.tc_splits, best_pers = s.tc_persistent, best_sp1 = 1;
     bool first = true, large = false;
     for (int mult : {1, 2, 4}) {
       const int bn = tc_tile_n(N, mult);
@@ -1826,7 +1847,22 @@ static void tune_schedule(Ctx& c, Schedule& s) {
       for (int pv : {0, 1}) {
         if (c.tc_persistent_option >= 0 && pv != c.tc_persistent_option) continue;
         pers = pv;
-        const float t1 = time_calls(c, kTuneReps, fwd);
+        // the F.V product: K splits only help when its tiles do not fill the GPU
+        int sp1_best = 1;
+        sp1 = 1;
+        float t1 = time_calls(c, kTuneReps, fwd);
+        const int64_t fwd_tiles = (int64_t)cdiv(N, bn) * c.tcF.blocks;
+        if (t1 < kTuneMaxMs && fwd_tiles < c.num_sms)
+          for (int cand : {2, 4}) {
+            if (cand > max_splits1) continue;
+            sp1 = cand;
+            const float t = time_calls(c, kTuneReps, fwd);
+            if (t < t1 * 0.97f) {
+              t1 = t;
+              sp1_best = cand;
+            }
+          }
+        sp1 = sp1_best;
         int sp_best = s.tc_splits;
         float t2 = time_calls(c, kTuneReps, [&] { trn(sp_best); });
         if (t1 + t2 < kTuneMaxMs)
@@ -1843,6 +1879,7 @@ static void tune_schedule(Ctx& c, Schedule& s) {
           best_bn = bn;
           best_sp = sp_best;
           best_pers = pv;
+          best_sp1 = sp1_best;
         }
         first = false;
         if (t1 + t2 >= kTuneMaxMs) large = true;
@@ -1850,6 +1887,7 @@ static void tune_schedule(Ctx& c, Schedule& s) {
       if (large) break;
     }
     s.tc_persistent = best_pers;
+    s.tc_splits1 = best_sp1;
     tc_configure(c, best_bn);
     s.tc_bn = best_bn;
     s.tc_splits = best_sp;
@@ -1921,7 +1959,14 @@ static void choose_schedule(Ctx& c) {
       g_sched[key] = s;
     }
   }
+  if (s.tc && c.tc_splits1_option > 0) s.tc_splits1 = c.tc_splits1_option;
   c.sched = s;
+  if (s.tc && s.tc_splits1 > 1) {
+    const size_t need1 = (size_t)s.tc_splits1 * (size_t)h.D * (size_t)h.N;
+    if (c.ypart.n != need1) c.ypart.alloc(need1);
+  } else {
+    c.ypart.release();
+  }
   if (c.precision == PQDTS_MIXED) {
     const size_t need = (size_t)(s.tc ? s.tc_splits : s.trn_splits) * (size_t)h.M * (size_t)h.N;
     if (c.hpart32.n != need) c.hpart32.alloc(need);
@@ -2371,6 +2416,9 @@ int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
       c->use_graphs = value != 0;
     } else if (n == "autotune") {
       c->autotune = value != 0;
+    } else if (n == "tc_splits1") {
+      if (value < -1 || value == 0 || value > 8) throw pqdts::Err(PQDTS_E_ARG, "tc_splits1 must be -1 or 1..8");
+      c->tc_splits1_option = (int)value;
     } else if (n == "tc_persistent") {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "tc_persistent must be -1, 0 or 1");
       c->tc_persistent_option = (int)value;
@@ -2400,6 +2448,7 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     else if (n == "sched.tc_splits") *value = s.tc_splits;
     else if (n == "sched.tc_bn") *value = s.tc_bn;
     else if (n == "sched.tc_persistent") *value = s.tc_persistent;
+    else if (n == "sched.tc_splits1") *value = s.tc_splits1;
     else if (n == "tc_persistent") *value = c->tc_persistent_option;
     else if (n == "tensor_cores") *value = c->tc_option;
     else if (n == "graphs.captured") *value = (int64_t)c->graphs.size();

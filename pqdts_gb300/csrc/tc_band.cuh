@@ -544,6 +544,35 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
   }
 }
 
+// Sum of `parts` FP32 partials (R x N row-major, R*N apart) -> transposed
+// split: hi[n * ld + r], lo[n * ld + r] (the first product with its K range
+// split, feeding the second product's B operand).
+__global__ void k_finish_t(const float* __restrict__ part, int parts, int R, int N, int64_t ld,
+                           __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
+                           const double* __restrict__ pred) {
+  if (pred != nullptr && pred[6] != 0.0) return;
+  __shared__ float t[32][33];
+  const int r0 = blockIdx.x * 32, n0 = blockIdx.y * 32;
+  const int64_t RN = (int64_t)R * N;
+  for (int rr = threadIdx.y; rr < 32; rr += blockDim.y) {
+    const int r = r0 + rr, n = n0 + threadIdx.x;
+    float v = 0.f;
+    if (r < R && n < N)
+      for (int q = 0; q < parts; ++q) v += part[q * RN + (int64_t)r * N + n];  // fixed order
+    t[rr][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int rr = threadIdx.y; rr < 32; rr += blockDim.y) {
+    const int n = n0 + rr, r = r0 + threadIdx.x;
+    if (n < N && r < R) {
+      const float x = t[threadIdx.x][rr];
+      const __nv_bfloat16 h = __float2bfloat16_rn(x);
+      hi[(int64_t)n * ld + r] = h;
+      lo[(int64_t)n * ld + r] = __float2bfloat16_rn(x - __bfloat162float(h));
+    }
+  }
+}
+
 // V (M x N row-major FP32) -> V^T split: hi[n * ld + i], lo[n * ld + i].
 __global__ void k_split_t(const float* __restrict__ V, int M, int N, int64_t ld, __nv_bfloat16* __restrict__ hi,
                           __nv_bfloat16* __restrict__ lo, const double* __restrict__ pred) {

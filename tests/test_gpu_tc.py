@@ -13,16 +13,19 @@ pytestmark = pytest.mark.gpu
 TC_REL = 1e-4
 
 
-def _tc_solver(inst, persistent=-1):
+def _tc_solver(inst, persistent=-1, splits1=-1):
     import pqdts_gb300 as pq
 
     s = pq.Solver(0)
     s.set_option("tensor_cores", 1)
     s.set_option("tc_persistent", persistent)
+    s.set_option("tc_splits1", splits1)
     s.set_instance(inst, pq.MIXED)
     assert s.get_option("sched.tc") == 1
     if persistent >= 0:
         assert s.get_option("sched.tc_persistent") == persistent
+    if splits1 > 0:
+        assert s.get_option("sched.tc_splits1") == splits1
     return s
 
 
@@ -88,3 +91,22 @@ def test_tc_mixed_solve_reaches_fp64_objective(built, tc_insts, persistent):
     s.close()
     assert abs(st["L"] - st64["L"]) <= 1e-8 * abs(st64["L"]), (st, st64)
     assert X.min() >= -1e-12 and np.max(np.abs(X.sum(1) - 1.0)) <= 1e-12
+
+
+@pytest.mark.parametrize("persistent", [0, 1])
+@pytest.mark.parametrize("which", ["tiny", "dense"])
+def test_tc_split_forward_product(built, tc_insts, which, persistent):
+    """F.V with its K range split (FP32 partials summed and split again by
+    k_finish_t) gives the same Hessian product to the split-BF16x3 bound."""
+    from oracle.oracle import Oracle
+
+    inst = tc_insts[which]
+    s = _tc_solver(inst, persistent, splits1=3)
+    o = Oracle.from_instance(inst)
+    rng = np.random.default_rng(12)
+    V = np.asfortranarray(rng.standard_normal((inst.M, inst.N)))
+    H = s.BF32(V)
+    H64 = o.BF(V)
+    s.close()
+    err = np.max(np.abs(H - H64)) / np.max(np.abs(H64))
+    assert err < TC_REL, err
