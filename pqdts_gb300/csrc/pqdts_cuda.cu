@@ -1402,22 +1402,29 @@ static void line_search_mixed(Ctx& c, bool stage2, double& alpha, double& dlalph
     }
     c.n_lsL += nb;
   };
-  // the slope probe alpha = dx (404, 450) as an objective change: a
+  // the slope probe alpha = dx (404, 450) as an objective change (a
   // difference of two FP64 objectives ~1e-9 apart is what the reference
-  // divides by dx; here it is computed directly
+  // divides by dx; here it is computed directly), screened together with
+  // the first two steps 1 and 0.75 (the full step is usually taken)
   double qa[kBatchLS], xmin[kBatchLS], dl[kBatchLS];
   qa[0] = 0.0 + kDx;
-  screen(qa, 1, dl, xmin);
+  qa[1] = 1.0;
+  qa[2] = 1.0 * 0.75;
+  screen(qa, 3, dl, xmin);
   LSState ls;
   ls.L0 = L0;
   ls.df = dl[0] / kDx;
   dlalpha = ls.df;
   bool screened_stop = false;
   double stop_a = 0.0;  // alpha of the probe where the screened sequence stopped
-  int batch = 2;        // probes per screening batch: 2 (the full step is usually taken), then 8
+  ls.next_a = qa[2] * 0.75;
+  for (int k = 1; k < 3 && !ls.done; ++k)
+    if (ls_take(c, ls, stage2, qa[k], ls.L0 + dl[k], xmin[k])) {
+      screened_stop = true;
+      stop_a = qa[k];
+    }
   while (!ls.done && ls.i <= kMaxLS) {
-    const int nb = std::min(batch, kMaxLS - ls.i + 1);
-    batch = kBatchLS;
+    const int nb = std::min(kBatchLS, kMaxLS - ls.i + 1);
     for (int k = 0; k < nb; ++k) {
       qa[k] = ls.next_a;
       ls.next_a = ls.next_a * 0.75;
@@ -1452,7 +1459,9 @@ static void line_search_mixed(Ctx& c, bool stage2, double& alpha, double& dlalph
 }
 
 // conv_test (1034-1067) on the context's X; leaves the full space selected.
-static double op_conv(Ctx& c, bool tprint) {
+// with_extra: sc[SC_TMP + 1] (written by the caller's earlier kernels) is
+// read back in the same transfer into c.pin[1].
+static double op_conv(Ctx& c, bool tprint, bool with_extra = false) {
   Scope s(c.timers, "conv_test");
   const int M = (int)c.h.M, N = (int)c.h.N;
   if (!c.fullspace) rebuild_x(c);
@@ -1469,7 +1478,7 @@ static double op_conv(Ctx& c, bool tprint) {
   } else {
     reduce_to(c, c.part.p, M, c.sc.p + SC_TMP);
   }
-  read_back(c, c.sc.p + SC_TMP, 1);
+  read_back(c, c.sc.p + SC_TMP, with_extra ? 2 : 1);
   const double conv = std::sqrt(c.pin[0] / ((double)N * (double)M));
   if (tprint && c.verbose) {
     std::vector<double> hl(M), hg((size_t)M * N);
@@ -1598,10 +1607,10 @@ static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
   }
   st.L0 = op_L(c);
   op_dL(c);
-  dot_dev(c, c.G.p, c.G.p, c.sc.p + SC_TMP);
-  read_back(c, c.sc.p + SC_TMP, 1);
-  st.norm_der = c.pin[0];
-  st.conv = op_conv(c, false);
+  // |der|^2 of this space's gradient, read back with conv_test's value
+  dot_dev(c, c.G.p, c.G.p, c.sc.p + SC_TMP + 1);
+  st.conv = op_conv(c, false, true);
+  st.norm_der = c.pin[1];
   st.outer++;
 }
 
