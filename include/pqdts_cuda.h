@@ -59,6 +59,8 @@ int pqdts_cuda_kernel_launches(pqdts_ctx* ctx, int64_t* count);
  *              run on the tensor cores (tcgen05, split-BF16x3, FP32
  *              accumulation) on compute capability 10.x devices; 0: FP32
  *              CUDA-core tiles.  Takes effect at the next set_problem.
+ *   "timers"   1 (default): GPU time per reference timer region
+ *              (pqdts_cuda_timer); 0: no events recorded.
  *   "tc_persistent" -1 (default, autotuned) / 0 / 1: the tensor-core kernel
  *              form (one CTA per output tile, or persistent with
  *              double-buffered accumulators); "tc_splits1" -1 (autotuned) or

@@ -13,6 +13,7 @@
 #include <array>
 #include <atomic>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -60,21 +61,32 @@ struct Err : std::runtime_error {
                     std::to_string(__LINE__) + ")");                                                    \
   } while (0)
 
+// Stream of the context whose entry point is running on this thread (set by
+// the C-ABI wrapper): device arrays are allocated and freed stream-ordered on
+// it (cudaMallocAsync / cudaFreeAsync), which, unlike cudaFree, does not
+// synchronise the device -- contexts on other threads (the batched solve's
+// workers) keep running.
+static thread_local cudaStream_t t_alloc_stream = nullptr;
+
 // Device array that keeps its allocation when a later problem fits in it
-// (cudaFree synchronises the whole device: a context reused for a stream of
-// instances, as the batched solve does, allocates only when one grows).
+// (a context reused for a stream of instances allocates only when one grows).
 template <typename T>
 struct DBuf {
   T* p = nullptr;
   size_t n = 0, cap = 0;
+  cudaStream_t s = nullptr;  // stream it was allocated on (null: cudaMalloc)
   DBuf() = default;
   DBuf(const DBuf&) = delete;
   DBuf& operator=(const DBuf&) = delete;
   ~DBuf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (s) cudaFreeAsync(p, s);
+      else cudaFree(p);
+    }
     p = nullptr;
     n = cap = 0;
+    s = nullptr;
   }
   void alloc(size_t count) {
     if (count == 0) count = 1;
@@ -83,7 +95,9 @@ struct DBuf {
       return;
     }
     release();
-    CK(cudaMalloc((void**)&p, count * sizeof(T)));
+    s = t_alloc_stream;
+    if (s) CK(cudaMallocAsync((void**)&p, count * sizeof(T), s));
+    else CK(cudaMalloc((void**)&p, count * sizeof(T)));
     n = cap = count;
   }
   void upload(const T* h, size_t count, cudaStream_t s, std::atomic<int64_t>* bytes) {
@@ -105,6 +119,7 @@ struct GpuTimers {
   std::vector<Pending> pending;
   std::vector<cudaEvent_t> pool;
   cudaStream_t st = nullptr;
+  bool enabled = true;  // Scope regions recorded (off: no events at all)
   int id_of(const char* n) {
     for (size_t i = 0; i < names.size(); ++i)
       if (names[i] == n) return (int)i;
@@ -212,10 +227,13 @@ struct GpuTimers {
 };
 
 struct Scope {
+  static constexpr int kOff = INT_MIN;
   GpuTimers& t;
   int tok;
-  Scope(GpuTimers& tt, const char* n) : t(tt), tok(tt.begin(n)) {}
-  ~Scope() { t.end(tok); }
+  Scope(GpuTimers& tt, const char* n) : t(tt), tok(tt.enabled ? tt.begin(n) : kOff) {}
+  ~Scope() {
+    if (tok != kOff) t.end(tok);
+  }
 };
 
 // One captured chunk of CG iterations, replayed with a single graph launch;
@@ -2012,9 +2030,17 @@ static void check_sizes(int64_t M, int64_t N, int64_t D) {
 using pqdts::Ctx;
 using pqdts::Err;
 
+// Restores the thread's allocation stream on every exit path.
+struct AllocStream {
+  cudaStream_t saved;
+  explicit AllocStream(cudaStream_t s) : saved(pqdts::t_alloc_stream) { pqdts::t_alloc_stream = s; }
+  ~AllocStream() { pqdts::t_alloc_stream = saved; }
+};
+
 template <typename F>
 static int guarded(Ctx* c, F&& f) {
   if (!c) return PQDTS_E_ARG;
+  AllocStream as(c->st);
   try {
     if (c->st) {
       cudaError_t e = cudaSetDevice(c->device);
@@ -2425,6 +2451,8 @@ int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
       c->use_graphs = value != 0;
     } else if (n == "autotune") {
       c->autotune = value != 0;
+    } else if (n == "timers") {
+      c->timers.enabled = value != 0;
     } else if (n == "tc_splits1") {
       if (value < -1 || value == 0 || value > 8) throw pqdts::Err(PQDTS_E_ARG, "tc_splits1 must be -1 or 1..8");
       c->tc_splits1_option = (int)value;
@@ -2447,6 +2475,7 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     const pqdts::Schedule& s = c->sched;
     if (n == "graphs") *value = c->use_graphs;
     else if (n == "autotune") *value = c->autotune;
+    else if (n == "timers") *value = c->timers.enabled;
     else if (n == "sched.fwd_tile") *value = s.fwd_tile;
     else if (n == "sched.trn_tile") *value = s.trn_tile;
     else if (n == "sched.trn_splits") *value = s.trn_splits;
@@ -2506,6 +2535,7 @@ int pqdts_cuda_solve_batch(int32_t device, int32_t n_inst, const int64_t* M, con
       rc = r;
       return;
     }
+    c->timers.enabled = false;  // no per-region events in the batch
     for (;;) {
       const int k = next++;
       if (k >= n_inst || rc.load() != PQDTS_OK) break;
