@@ -53,3 +53,12 @@ def test_cli_usage_without_args(built):
 
     r = subprocess.run([pq.CLI_PATH], capture_output=True, text=True)
     assert r.returncode == 1 and "usage" in r.stderr
+
+
+def test_fortran_module_binds_every_entry_point():
+    """pqdts_gb300/fortran/pqdts_cuda_mod.f90 declares an iso_c_binding
+    interface for each function of the C header (no Fortran compiler here:
+    checked by name)."""
+    src = open(os.path.join(ROOT, "pqdts_gb300", "fortran", "pqdts_cuda_mod.f90")).read()
+    bound = set(re.findall(r'bind\(C,\s*name="(pqdts_cuda_\w+)"\)', src))
+    assert bound == set(_declared()), (set(_declared()) - bound, bound - set(_declared()))
