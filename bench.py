@@ -545,7 +545,7 @@ def run_workload(name, args):
                         "cg_total": sum(x["cg"] for x in stm), "max_rel_objective_vs_fp64": float(rel.max()),
                         "instances_at_target": int((Lm <= L64 * (1.0 + OBJ_REL)).sum())}
         out["mixed_speedup_vs_fp64"] = t64 / tmix
-        out["workers"] = int(os.environ.get("PQDTS_BATCH_WORKERS", "8"))
+        out["workers"] = int(os.environ.get("PQDTS_BATCH_WORKERS", "0")) or min(16, os.cpu_count() or 1)
         if args.batch_sequential:
             # the same FP64 solves one after another through one context
             t0 = time.perf_counter()

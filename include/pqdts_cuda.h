@@ -197,8 +197,9 @@ int pqdts_cuda_timer(pqdts_ctx* ctx, const char* name, double* seconds, int64_t*
  * X holds sum_k M[k]*N[k] doubles (column-major per instance, in order),
  * starting points on entry and results on exit.  target_L (may be null):
  * per-instance objective targets as pqdts_cuda_set_objective_target.
- * stats: PQDTS_NSTATS per instance.  Host workers (8, or the environment
- * variable PQDTS_BATCH_WORKERS, at most one per instance) each own a
+ * stats: PQDTS_NSTATS per instance.  Host workers (the host's hardware
+ * threads up to 16, or the environment variable PQDTS_BATCH_WORKERS; at
+ * most one per instance) each own a
  * context and stream and take instances in order, so instances overlap on
  * the device; each context's CG chunks replay as CUDA graphs and instances
  * of one size bucket share one autotuned launch schedule. */

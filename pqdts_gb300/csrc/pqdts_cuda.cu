@@ -2521,8 +2521,9 @@ int pqdts_cuda_solve_batch(int32_t device, int32_t n_inst, const int64_t* M, con
   // context and stream, so the instances' kernels overlap on the device.
   std::vector<int64_t> xoff(n_inst + 1, 0);
   for (int k = 0; k < n_inst; ++k) xoff[k + 1] = xoff[k] + M[k] * N[k];
-  // workers: PQDTS_BATCH_WORKERS (default 8), at most one per instance
-  int workers = 8;
+  // workers: PQDTS_BATCH_WORKERS (default: the host's hardware threads, at
+  // most 16), at most one per instance
+  int workers = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
   if (const char* e = std::getenv("PQDTS_BATCH_WORKERS")) workers = std::max(1, std::min(64, std::atoi(e)));
   workers = std::min<int>(n_inst, workers);
   std::atomic<int> next{0};
