@@ -42,6 +42,10 @@ def _instances():
         # every entry kept: the dense-F variant
         "dense": synth.make_instance(M=300, N=40, D=300, xmax=250.0, eta=0.85, shots=10**6, gamma=1e-4, eps=1e-6,
                                      seed=6, dense=True),
+        # probe rows whose window lies beyond M (rows 117.. empty: whole
+        # 128-row blocks without a band), gamma = 0, N = 10
+        "empty_rows": synth.make_instance(M=60, N=10, D=400, xmax=500.0, eta=0.85, shots=10**5, gamma=0.0, eps=1e-6,
+                                          seed=9),
     }
 
 
@@ -50,7 +54,7 @@ def tc_insts():
     return _instances()
 
 
-@pytest.mark.parametrize("which", ["tiny", "cfg1", "medium", "dense"])
+@pytest.mark.parametrize("which", ["tiny", "cfg1", "medium", "dense", "empty_rows"])
 @pytest.mark.parametrize("full", [True, False])
 @pytest.mark.parametrize("persistent", [0, 1])
 def test_tc_hessian_product_matches_fp64(built, tc_insts, which, full, persistent):
