@@ -34,3 +34,12 @@ def small():
     from pqdts_gb300 import synth
 
     return synth.make_instance(M=80, N=12, D=160, xmax=60.0, eta=0.85, shots=10**5, gamma=1e-3, eps=1e-6, seed=7)
+
+
+@pytest.fixture(scope="session")
+def empty_rows():
+    """Probe rows 117..399 have no band inside M (x_d beyond the last
+    photon number): empty F rows and whole empty 128-row blocks; gamma = 0."""
+    from pqdts_gb300 import synth
+
+    return synth.make_instance(M=60, N=10, D=400, xmax=500.0, eta=0.85, shots=10**5, gamma=0.0, eps=1e-6, seed=9)

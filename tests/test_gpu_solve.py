@@ -38,7 +38,7 @@ def _solve_gpu(inst, precision=0, mode=2, maxiter=200, eps=None):
         return s.get_x(), st, s.kernel_launches()
 
 
-@pytest.mark.parametrize("which", ["cfg1", "small"])
+@pytest.mark.parametrize("which", ["cfg1", "small", "empty_rows"])
 def test_fp64_solve_matches_oracle(built, request, which):
     from oracle.oracle import Oracle
 
