@@ -1007,11 +1007,13 @@ static void hvp32(Ctx& c, CGBufs<float>& b, const int8_t* ik, bool with_dot, con
                        pred, parts, 0, (int64_t)M * N, parts);
   }
   const int tb = std::min(256, std::max(32, cdiv(N, 32) * 32));
-  // p.Hp -> sc[SC_V2] by the epilogue's last row block
+  // (one block per row: a grid-completion counter over M blocks costs more
+  // than the separate reduction)
   k_hvp_epi32<<<M, tb, 0, c.st>>>(c.hpart32.p, b.p.p, c.fullspace ? nullptr : b.rs.p, c.maxr.p, c.fullspace ? 0 : 1,
                                   (float)(2.0 * c.h.gam), ik, M, N, b.Hp.p, with_dot ? c.part.p : nullptr, pred,
-                                  parts, with_dot ? c.sc.p + SC_V2 : nullptr, c.counters.p);
+                                  parts);
   post_launch(c);
+  if (with_dot) reduce_to(c, c.part.p, M, c.sc.p + SC_V2, 1, false, 0.0, pred);
 }
 
 // A chunk of CG iterations captured as a CUDA graph (on first use of its
@@ -1197,12 +1199,12 @@ static void cg_solve(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, double bdfa
         k_cg_pupdate<T><<<g, 256, 0, c.st>>>(c.sc.p, MN, b.p.p, b.z.p);
         post_launch(c);
       } else {
-        k_cg_lift<T><<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(c.sc.p, 1, M, N, b.p.p, b.z.p, c.maxr.p, b.V.p,
+        k_cg_lift<T><<<cdiv(M, 32), kLiftThreads, 0, c.st>>>(c.sc.p, 1, M, N, b.p.p, b.z.p, c.maxr.p, b.V.p,
                                                                        b.rs.p);
         post_launch(c);
       }
     } else if (!c.fullspace) {
-      k_cg_lift<T><<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(nullptr, 0, M, N, b.p.p, b.z.p, c.maxr.p, b.V.p,
+      k_cg_lift<T><<<cdiv(M, 32), kLiftThreads, 0, c.st>>>(nullptr, 0, M, N, b.p.p, b.z.p, c.maxr.p, b.V.p,
                                                                      b.rs.p);
       post_launch(c);
     }
@@ -2281,7 +2283,7 @@ int pqdts_cuda_BF(pqdts_ctx* c, const double* V, double* HV) {
     auto& b = c->cg64;
     CK(cudaMemcpyAsync(b.p.p, rm.data(), rm.size() * 8, cudaMemcpyHostToDevice, c->st));
     if (!c->fullspace) {
-      pqdts::k_cg_lift<double><<<pqdts::cdiv(M, pqdts::kRowThreads), pqdts::kRowThreads, 0, c->st>>>(
+      pqdts::k_cg_lift<double><<<pqdts::cdiv(M, 32), pqdts::kLiftThreads, 0, c->st>>>(
           nullptr, 0, (int)M, (int)N, b.p.p, b.z.p, c->maxr.p, b.V.p, b.rs.p);
       pqdts::post_launch(*c);
     }
