@@ -1810,6 +1810,16 @@ static Schedule heuristic_schedule(const HostProblem& h) {
   return s;
 }
 
+// The Hessian row epilogue over `parts` partials (full space, no mask), as
+// the CG runs it after the transposed product: part of that product's cost.
+static void tune_epilogue(Ctx& c, int parts) {
+  const int M = (int)c.h.M, N = (int)c.h.N;
+  const int tb = std::min(256, std::max(32, cdiv(N, 32) * 32));
+  k_hvp_epi32<<<M, tb, 0, c.st>>>(c.hpart32.p, c.cg32.p.p, nullptr, c.maxr.p, 0, (float)(2.0 * c.h.gam), nullptr, M, N,
+                                  c.cg32.Hp.p, c.part.p, nullptr, parts);
+  post_launch(c);
+}
+
 static void tune_schedule(Ctx& c, Schedule& s) {
   const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
   const int64_t MN = (int64_t)M * N;
@@ -1862,9 +1872,10 @@ static void tune_schedule(Ctx& c, Schedule& s) {
     const int max_splits1 = (int)std::max<int64_t>(1, std::min<int64_t>(4, ((int64_t)1 << 30) / (DN * 4)));
     if (max_splits1 > 1) c.ypart.alloc((size_t)max_splits1 * DN);
     auto fwd = [&] { tc_forward(c, sp1, pers, nullptr); };
-    auto trn = [&](int sp) {
+    auto trn = [&](int sp) {  // the F^T product and the epilogue that sums its sp partials
       tc_product(c, c.tcFt, c.map_yt_hi, c.map_yt_lo, M, sp, 0, 1.0f, c.hpart32.p, nullptr, nullptr, 0, nullptr,
                  pers);
+      tune_epilogue(c, sp);
     };
     float best = 0.0f;
     int best_bn = s.tc_bn, best_sp = s.tc_splits, best_pers = s.tc_persistent, best_sp1 = 1;
@@ -1941,9 +1952,10 @@ static void tune_schedule(Ctx& c, Schedule& s) {
   // transposed product: tile x K splits, partials of at most 1 GiB
   const int max_splits = (int)std::max<int64_t>(1, std::min<int64_t>(8, ((int64_t)1 << 30) / (MN * 4)));
   c.hpart32.alloc((size_t)std::max(max_splits, s.trn_splits) * MN);
-  auto trn = [&](int tile, int sp) {
+  auto trn = [&](int tile, int sp) {  // the F^T product and the epilogue that sums its sp partials
     launch_band_gemm32(c, tile, c.tlo.p, c.tw.p, c.toff.p, c.tbval32.p, b.R2.p, M, N, 1.0f, c.hpart32.p, nullptr,
                        sp, 0, MN, sp);
+    tune_epilogue(c, sp);
   };
   best = time_calls(c, kTuneReps, [&] { trn(s.trn_tile, s.trn_splits); });
   if (best < kTuneMaxMs)
