@@ -936,10 +936,13 @@ static void tc_forward(Ctx& c, int splits1, int persistent, const double* pred) 
 // The Hessian product pair on the tensor cores: V -> V^T split, then
 // (2 F.V)^T split (written by the first product's epilogue), then the
 // partials of F^T.(2 F.V) in hpart32 (tc_splits of them).
-static void tc_hvp_products(Ctx& c, const float* src, const double* pred) {
+static void tc_hvp_products(Ctx& c, const float* src, const double* pred, bool presplit) {
   const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
-  k_split_t<<<dim3(cdiv(M, 32), cdiv(N, 32)), dim3(32, 8), 0, c.st>>>(src, M, N, c.tc_mp, c.vt_hi.p, c.vt_lo.p, pred);
-  post_launch(c);
+  if (!presplit) {
+    k_split_t<<<dim3(cdiv(M, 32), cdiv(N, 32)), dim3(32, 8), 0, c.st>>>(src, M, N, c.tc_mp, c.vt_hi.p, c.vt_lo.p,
+                                                                         pred);
+    post_launch(c);
+  }
   tc_forward(c, c.sched.tc_splits1, c.sched.tc_persistent, pred);
   tc_product(c, c.tcFt, c.map_yt_hi, c.map_yt_lo, M, c.sched.tc_splits, 0, 1.0f, c.hpart32.p, nullptr, nullptr, 0,
              pred, c.sched.tc_persistent);
@@ -990,13 +993,15 @@ static int heuristic_tile(int R, int N, int nz = 1) {
 
 // Mixed precision Hessian product Hp = H p in FP32 with the tiled band
 // products (F.V then F^T.(2O)) and the row epilogue; p.Hp -> sc[SC_V2].
-static void hvp32(Ctx& c, CGBufs<float>& b, const int8_t* ik, bool with_dot, const double* pred) {
+// presplit: V's transposed split is already in place (k_lift_split32).
+static void hvp32(Ctx& c, CGBufs<float>& b, const int8_t* ik, bool with_dot, const double* pred,
+                  bool presplit = false) {
   const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
   const float* src = c.fullspace ? b.p.p : b.V.p;
   require(c.hpart32.p, "split-K partials");
   int parts;
   if (c.sched.tc) {
-    tc_hvp_products(c, src, pred);
+    tc_hvp_products(c, src, pred, presplit);
     parts = c.sched.tc_splits;
   } else {
     launch_band_gemm32(c, c.sched.fwd_tile, c.flo.p, c.fw.p, c.foff.p, c.fval32.p, src, D, N, 2.0f, b.R2.p, pred);
@@ -1118,8 +1123,15 @@ static void cg_solve32(Ctx& c, double bdfac) {
     l.s("positivity constraints").i8(nact).s("active of").i8(MN).r8((double)nact / (double)MN).print();
   }
   const int lift_blocks = cdiv((int64_t)M * 32, 256);
+  const bool tc = c.sched.tc != 0;
   auto iteration = [&](bool first) {
-    if (c.fullspace) {
+    if (tc) {
+      // p update, lift and the first product's operand split in one pass
+      k_lift_split32<<<cdiv(M, 32), 256, 0, c.st>>>(first ? nullptr : c.sc.p, first ? 0 : 1, c.fullspace ? 0 : 1, M,
+                                                    N, b.p.p, b.z.p, c.maxr.p, b.rs.p, c.tc_mp, c.vt_hi.p,
+                                                    c.vt_lo.p);
+      post_launch(c);
+    } else if (c.fullspace) {
       if (!first) {
         k_cg_pupdate<float><<<g, 256, 0, c.st>>>(c.sc.p, MN, b.p.p, b.z.p);
         post_launch(c);
@@ -1131,7 +1143,7 @@ static void cg_solve32(Ctx& c, double bdfac) {
     }
     {
       Scope sb(c.timers, "BF");
-      hvp32(c, b, c.ik.p, true, c.sc.p);
+      hvp32(c, b, c.ik.p, true, c.sc.p, tc);
     }
     // the step; its last block sums r.z, r.r and advances the CG scalars
     k_cg_step32<<<g, 256, 0, c.st>>>(c.sc.p, c.rsq32.p, M, N, b.p.p, b.Hp.p, b.sn.p, b.r.p, b.z.p, c.part.p,
