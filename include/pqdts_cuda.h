@@ -59,6 +59,9 @@ int pqdts_cuda_kernel_launches(pqdts_ctx* ctx, int64_t* count);
  *              run on the tensor cores (tcgen05, split-BF16x3, FP32
  *              accumulation) on compute capability 10.x devices; 0: FP32
  *              CUDA-core tiles.  Takes effect at the next set_problem.
+ *   "rows_kernels" -1 (default, autotuned) / 0 / 1: the FP64 banded products
+ *              in their row-flattened form (every lane busy when N is not a
+ *              multiple of 32; the same bits) where it applies.
  *   "timers"   1 (default): GPU time per reference timer region
  *              (pqdts_cuda_timer); 0: no events recorded.
  *   "tc_persistent" -1 (default, autotuned) / 0 / 1: the tensor-core kernel
@@ -73,6 +76,7 @@ int pqdts_cuda_set_option(pqdts_ctx* ctx, const char* name, int64_t value);
  * "sched.trans_threads", "sched.trans_cols" (FP64 F^T product block shape),
  * "sched.tuned" (1 = timed, 0 = heuristic), "sched.tc" (1 = tensor-core
  * Hessian products in use), "sched.tc_bn" (their N tile width),
+ * "sched.fwd_rows", "sched.trans_rows" (row-flattened FP64 products in use),
  * "sched.tc_splits" (K segments of their F^T product), "sched.tc_splits1"
  * (of their F.V product), "sched.tc_persistent" (kernel form),
  * "graphs.captured" (graphs held). */

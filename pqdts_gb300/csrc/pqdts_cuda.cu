@@ -260,6 +260,8 @@ struct Schedule {
   int trn_splits = 1;     // ... with its K range split in this many segments
   int trans_threads = 0;  // FP64 F^T product: threads per row block (0 = heuristic)
   int trans_cols = 0;     // ... and columns per thread
+  int trans_rows = 0;     // 1: FP64 F^T product row-flattened (k_trans_rows)
+  int fwd_rows = 0;       // 1: FP64 F.X product row-flattened (k_fwd_rows)
   int tuned = 0;          // 1 = picked by timing, 0 = heuristic
   int tc = 0;             // mixed CG products on the tensor cores (split-BF16x3)
   int tc_splits = 1;      // K segments of their F^T product
@@ -312,6 +314,7 @@ struct pqdts_ctx {
   pqdts::DBuf<double> fval, tval, bdiag, P;
   pqdts::DBuf<float> fval32, tval32, tbval32, rsq32;
   pqdts::DBuf<double> sqd;  // sqrt(bdfac * Bdiag) per row, FP64 CG step
+  bool t_contiguous = false;  // every column of F supported on a contiguous range of d
   pqdts::DBuf<unsigned> counters;  // grid-completion counters of fused reductions (kept at 0 between launches)
   pqdts::DBuf<int32_t> tlo, tw;
   pqdts::DBuf<int64_t> toff;
@@ -362,6 +365,7 @@ struct pqdts_ctx {
   int tc_option = -1;
   int tc_persistent_option = -1;  // -1 autotuned, 0 one CTA per tile, 1 persistent
   int tc_splits1_option = -1;     // -1 autotuned, else the K segments of the tensor-core F.V product
+  int rows_option = -1;           // row-flattened FP64 products: -1 autotuned, 0 never, 1 always (where they apply)
   int num_sms = 0;
   bool tc_ready = false;
   int tc_bn = 0, tc_stages = 0;
@@ -443,6 +447,11 @@ static void setup_device(Ctx& c) {
   c.tval.upload(h.tval.data(), h.tval.size(), c.st, &c.h2d);
   c.bdiag.upload(h.bdiag.data(), M, c.st, &c.h2d);
   c.P.upload(h.P.data(), h.P.size(), c.st, &c.h2d);
+  c.t_contiguous = true;
+  for (int64_t i = 0; i < M && c.t_contiguous; ++i) {
+    const int64_t e0 = h.tptr[i], e1 = h.tptr[i + 1];
+    if (e1 > e0 && h.tidx[e1 - 1] - h.tidx[e0] + 1 != e1 - e0) c.t_contiguous = false;
+  }
   if (c.precision == PQDTS_MIXED) {
     std::vector<float> f32(h.fval.begin(), h.fval.end());
     c.fval32.upload(f32.data(), f32.size(), c.st, &c.h2d);
@@ -561,15 +570,46 @@ static void require(const void* p, const char* what) {
   if (p == nullptr) throw Err(PQDTS_E_STATE, std::string("internal: device buffer ") + what + " is not allocated");
 }
 
+// Rows per block of the row-flattened products: the most busy lanes with
+// RB*N <= 1024 threads and RB <= 32; 0 when N is outside [32, 1024].
+static int rows_per_block(int N) {
+  if (N < 32 || N > 1024) return 0;
+  int best = 0;
+  double beff = 0.0;
+  for (int rb = 1; rb <= 32 && rb * N <= 1024; ++rb) {
+    const int t = rb * N;
+    const double eff = (double)t / (32.0 * ((t + 31) / 32));
+    if (eff > beff + 1e-12) {
+      beff = eff;
+      best = rb;
+    }
+  }
+  return best;
+}
+
+// F.X (B stacked inputs, xstride apart) with the epilogue MODE of k_fwd, in
+// the context's form: column-tiled, or row-flattened (rows = 1; the same bits).
+template <typename T, int MODE>
+static void launch_fwd(Ctx& c, const T* fv, const T* X, int64_t xstride, const double* P, T* R, int B,
+                       const double* pred, int rows = -1) {
+  const int N = (int)c.h.N, D = (int)c.h.D;
+  DevBands bd = bands_of(c);
+  const int RB = rows_per_block(N);
+  if ((rows < 0 ? c.sched.fwd_rows : rows) && RB > 0) {
+    const int threads = cdiv((int64_t)RB * N, 32) * 32;
+    k_fwd_rows<T, MODE><<<dim3(cdiv(D, RB), B), threads, 0, c.st>>>(bd, fv, X, xstride, P, R, RB, pred);
+  } else {
+    k_fwd<T, MODE><<<dim3(cdiv(N, kBX), cdiv(D, kBY), B), dim3(kBX, kBY), 0, c.st>>>(bd, fv, X, xstride, P, R, nullptr,
+                                                                                    pred);
+  }
+  post_launch(c);
+}
+
 static void objective_stack(Ctx& c, const double* Xs, int B) {
   const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
   require(c.Rst.p, "Rst");
   if (B < 1 || B > kBatchLS) throw Err(PQDTS_E_STATE, "internal: candidate batch out of range");
-  DevBands bd = bands_of(c);
-  dim3 grid(cdiv(N, kBX), cdiv(D, kBY), B);
-  k_fwd<double, 3><<<grid, dim3(kBX, kBY), 0, c.st>>>(bd, c.fval.p, Xs, (int64_t)M * N, c.P.p, c.Rst.p, nullptr,
-                                                      nullptr);
-  post_launch(c);
+  launch_fwd<double, 3>(c, c.fval.p, Xs, (int64_t)M * N, c.P.p, c.Rst.p, B, nullptr);
   k_rowchain_resid<<<dim3(cdiv(D, kRowThreads), B), kRowThreads, 0, c.st>>>(c.Rst.p, c.flo.p, D, N, 1.0, c.srow.p);
   post_launch(c);
   objective_combine(c, Xs, B);
@@ -597,11 +637,7 @@ static void rebuild_x(Ctx& c) {
 // for this version of X.
 static void ensure_R(Ctx& c) {
   if (c.R_ver == c.xver) return;
-  const int N = (int)c.h.N, D = (int)c.h.D;
-  DevBands bd = bands_of(c);
-  k_fwd<double, 0><<<dim3(cdiv(N, kBX), cdiv(D, kBY), 1), dim3(kBX, kBY), 0, c.st>>>(bd, c.fval.p, c.X.p, 0, c.P.p,
-                                                                                     c.R.p, nullptr, nullptr);
-  post_launch(c);
+  launch_fwd<double, 0>(c, c.fval.p, c.X.p, 0, c.P.p, c.R.p, 1, nullptr);
   c.R_ver = c.xver;
 }
 
@@ -628,7 +664,10 @@ static double op_L(Ctx& c) {
 // lanes (an idle lane still costs its FP64 issue slot).
 struct TransShape {
   int threads, C;
+  int rows = 0;  // 1: the row-flattened kernel (k_trans_rows)
 };
+
+
 static TransShape trans_shape(int N) {
   // fewest passes over the CSR row first (each pass re-reads it), then the
   // fewest idle lanes, then the fewest columns per thread (more warps).
@@ -656,6 +695,14 @@ static void launch_trans_shape(Ctx& c, TransShape sh, const T* tv, const T* R, c
                                T* Gf = nullptr) {
   const int M = (int)c.h.M;
   DevBands bd = bands_of(c);
+  const int RB = rows_per_block((int)c.h.N);
+  if (sh.rows && W == nullptr && c.t_contiguous && RB > 0) {
+    const int threads = cdiv((int64_t)RB * c.h.N, 32) * 32;
+    k_trans_rows<T, HVP><<<cdiv(M, RB), threads, 0, c.st>>>(bd, tv, RB, R, V, rs, c.maxr.p, reduced, c2gam, ik, G,
+                                                            pred, Gf);
+    post_launch(c);
+    return;
+  }
   switch (sh.C) {
     case 1:
       k_trans<T, HVP, 1><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf);
@@ -677,8 +724,9 @@ static void launch_trans_shape(Ctx& c, TransShape sh, const T* tv, const T* R, c
 template <typename T, bool HVP>
 static void launch_trans(Ctx& c, const T* tv, const T* R, const T* V, const T* rs, int reduced, T c2gam,
                          const int8_t* ik, T* G, const T* W, double* dpart, const double* pred, T* Gf = nullptr) {
-  const TransShape sh = c.sched.trans_threads > 0 ? TransShape{c.sched.trans_threads, c.sched.trans_cols}
-                                                  : trans_shape((int)c.h.N);
+  TransShape sh = c.sched.trans_threads > 0 ? TransShape{c.sched.trans_threads, c.sched.trans_cols}
+                                            : trans_shape((int)c.h.N);
+  sh.rows = c.sched.trans_rows;
   launch_trans_shape<T, HVP>(c, sh, tv, R, V, rs, reduced, c2gam, ik, G, W, dpart, pred, Gf);
 }
 
@@ -746,12 +794,9 @@ static void dot2_exact(Ctx& c, const double* a, const double* b, double* out_ab,
 template <typename T>
 static void hvp(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, const int8_t* ik, bool with_dot,
                 const double* pred = nullptr) {
-  const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
-  DevBands bd = bands_of(c);
+  const int M = (int)c.h.M;
   const T* src = c.fullspace ? b.p.p : b.V.p;
-  k_fwd<T, 1><<<dim3(cdiv(N, kBX), cdiv(D, kBY), 1), dim3(kBX, kBY), 0, c.st>>>(bd, fv, src, 0, nullptr, b.R2.p,
-                                                                                nullptr, pred);
-  post_launch(c);
+  launch_fwd<T, 1>(c, fv, src, 0, nullptr, b.R2.p, 1, pred);
   launch_trans<T, true>(c, tv, b.R2.p, b.p.p, c.fullspace ? nullptr : b.rs.p, c.fullspace ? 0 : 1,
                         (T)(2.0 * c.h.gam), ik, b.Hp.p, with_dot ? b.p.p : nullptr, with_dot ? c.part.p : nullptr,
                         pred);
@@ -1770,7 +1815,7 @@ static void solve(Ctx& c, int mode, int maxiiter, double conv_thres, int start_s
 // one bucket (a resampled or gamma-swept batch) are tuned once.
 // ---------------------------------------------------------------------------
 static std::mutex g_sched_mu;
-static std::map<std::array<int64_t, 8>, Schedule> g_sched;
+static std::map<std::array<int64_t, 10>, Schedule> g_sched;
 
 static int ilog2_ceil(int64_t v) {
   int k = 0;
@@ -1867,6 +1912,21 @@ static void tune_schedule(Ctx& c, Schedule& s) {
           s.trans_cols = cand.C;
         }
       }
+    }
+    // the row-flattened forms (same bits), where they apply
+    if (c.rows_option != 0 && rows_per_block(N) > 0) {
+      if (c.t_contiguous) {
+        TransShape rw{s.trans_threads, s.trans_cols};
+        rw.rows = 1;
+        const float t = time_calls(c, kTuneReps, [&] { run(rw); });
+        s.trans_rows = (c.rows_option == 1 || t < best) ? 1 : 0;
+      }
+      auto fwd64 = [&](int rows) {
+        launch_fwd<double, 1>(c, c.fval.p, b.p.p, 0, nullptr, b.R2.p, 1, nullptr, rows);
+      };
+      const float t0 = time_calls(c, kTuneReps, [&] { fwd64(0); });
+      const float t1 = t0 < kTuneMaxMs ? time_calls(c, kTuneReps, [&] { fwd64(1); }) : t0;
+      s.fwd_rows = (c.rows_option == 1 || t1 < t0) ? 1 : 0;
     }
   }
   if (c.precision != PQDTS_MIXED) return;
@@ -1998,9 +2058,10 @@ static void choose_schedule(Ctx& c) {
   }
   if (c.autotune) {
     const int64_t wavg = h.D > 0 ? std::max<int64_t>(1, h.nnz() / h.D) : 1;
-    const std::array<int64_t, 8> key{c.device,        c.precision,      h.N,
-                                     ilog2_ceil(h.M),  ilog2_ceil(h.D),  ilog2_ceil(wavg),
-                                     (int64_t)s.tc,    (int64_t)c.tc_persistent_option};
+    const std::array<int64_t, 10> key{c.device,        c.precision,      h.N,
+                                      ilog2_ceil(h.M),  ilog2_ceil(h.D),  ilog2_ceil(wavg),
+                                      (int64_t)s.tc,    (int64_t)c.tc_persistent_option,
+                                      (int64_t)c.rows_option, (int64_t)c.t_contiguous};
     std::lock_guard<std::mutex> lk(g_sched_mu);
     auto it = g_sched.find(key);
     if (it != g_sched.end()) {
@@ -2013,6 +2074,10 @@ static void choose_schedule(Ctx& c) {
     }
   }
   if (s.tc && c.tc_splits1_option > 0) s.tc_splits1 = c.tc_splits1_option;
+  if (c.rows_option >= 0 && rows_per_block((int)h.N) > 0) {
+    s.fwd_rows = c.rows_option;
+    s.trans_rows = c.rows_option && c.t_contiguous ? 1 : 0;
+  }
   c.sched = s;
   if (s.tc && s.tc_splits1 > 1) {
     const size_t need1 = (size_t)s.tc_splits1 * (size_t)h.D * (size_t)h.N;
@@ -2283,13 +2348,9 @@ int pqdts_cuda_dL(pqdts_ctx* c, double* G) {
 int pqdts_cuda_redO(pqdts_ctx* c, double* O) {
   return guarded(c, [&] {
     pqdts::need_problem(*c);
-    const int N = (int)c->h.N, D = (int)c->h.D;
-    pqdts::DevBands bd = pqdts::bands_of(*c);
+    const int64_t N = c->h.N, D = c->h.D;
     // R = 2*O - 0 via the Hessian epilogue, halved on the host (exact).
-    pqdts::k_fwd<double, 1><<<dim3(pqdts::cdiv(N, pqdts::kBX), pqdts::cdiv(D, pqdts::kBY), 1),
-                              dim3(pqdts::kBX, pqdts::kBY), 0, c->st>>>(bd, c->fval.p, c->X.p, 0, nullptr, c->R.p,
-                                                                        nullptr, nullptr);
-    pqdts::post_launch(*c);
+    pqdts::launch_fwd<double, 1>(*c, c->fval.p, c->X.p, 0, nullptr, c->R.p, 1, nullptr);
     c->R_ver = -1;  // R now holds 2*O, not 2*(O - P)
     CK(cudaMemcpyAsync(O, c->R.p, (size_t)D * N * 8, cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
@@ -2479,6 +2540,9 @@ int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
       c->autotune = value != 0;
     } else if (n == "timers") {
       c->timers.enabled = value != 0;
+    } else if (n == "rows_kernels") {
+      if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "rows_kernels must be -1, 0 or 1");
+      c->rows_option = (int)value;
     } else if (n == "tc_splits1") {
       if (value < -1 || value == 0 || value > 8) throw pqdts::Err(PQDTS_E_ARG, "tc_splits1 must be -1 or 1..8");
       c->tc_splits1_option = (int)value;
@@ -2513,6 +2577,9 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     else if (n == "sched.tc_bn") *value = s.tc_bn;
     else if (n == "sched.tc_persistent") *value = s.tc_persistent;
     else if (n == "sched.tc_splits1") *value = s.tc_splits1;
+    else if (n == "sched.fwd_rows") *value = s.fwd_rows;
+    else if (n == "sched.trans_rows") *value = s.trans_rows;
+    else if (n == "rows_kernels") *value = c->rows_option;
     else if (n == "tc_persistent") *value = c->tc_persistent_option;
     else if (n == "tensor_cores") *value = c->tc_option;
     else if (n == "graphs.captured") *value = (int64_t)c->graphs.size();

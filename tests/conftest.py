@@ -43,3 +43,12 @@ def empty_rows():
     from pqdts_gb300 import synth
 
     return synth.make_instance(M=60, N=10, D=400, xmax=500.0, eta=0.85, shots=10**5, gamma=0.0, eps=1e-6, seed=9)
+
+
+@pytest.fixture(scope="session")
+def mid():
+    """N = 40 (not a multiple of 32, >= 32): the row-flattened FP64 products
+    apply (4 rows x 40 columns = 5 full warps per block)."""
+    from pqdts_gb300 import synth
+
+    return synth.make_instance(M=300, N=40, D=600, xmax=250.0, eta=0.85, shots=10**6, gamma=1e-4, eps=1e-6, seed=11)

@@ -163,3 +163,20 @@ def test_option_errors(built):
         with pytest.raises(pq.PqdtsError):
             s.get_option("sched.nothing")
         assert s.get_option("graphs") == 1 and s.get_option("autotune") == 1
+
+
+@pytest.mark.parametrize("rows", [1, 0])
+def test_row_flattened_products_bitwise(built, mid, rows):
+    """The row-flattened FP64 products (every lane busy for N = 40) give the
+    oracle's trajectory bit for bit, as the column-tiled ones do."""
+    import pqdts_gb300 as pq
+    from oracle.oracle import Oracle
+
+    with pq.Solver(0) as s:
+        s.set_option("rows_kernels", rows)
+        s.set_instance(mid)
+        assert s.get_option("sched.fwd_rows") == rows and s.get_option("sched.trans_rows") == rows
+        st = s.solve(mode=2, maxiter=200, eps=mid.eps)
+        X = s.get_x()
+    Xo, so = Oracle.from_instance(mid).solve(mode=2, maxiter=200, eps=mid.eps)
+    assert st["L"] == so["L"] and st["cg"] == so["cg"] and np.array_equal(X, Xo)
