@@ -450,7 +450,8 @@ def run_ours(args):
 def run_profile_case(case):
     """Launches for ncu on the benchmark workload.
       fp64 / mixed: the Hessian product (3x BF resp. BF32), then 3x dL and
-        3x L at a random feasible X -- real banded-product launches only;
+        3x L at a random feasible X -- real banded-product launches only
+        (fp64: row-flattened products, no autotuning launches);
       solve64 / solvemix: one full benchmark solve (the launch list)."""
     import numpy as np
 
@@ -476,6 +477,11 @@ def run_profile_case(case):
     inst = synth.make_config(CONFIG, seed=0)
     prec = pq.MIXED if case in ("mixed", "solvemix") else pq.FP64
     with pq.Solver(0) as s:
+        if case == "fp64":
+            # no autotuning launches before the captured ones; the
+            # row-flattened products, the form the autotuner picks here
+            s.set_option("autotune", 0)
+            s.set_option("rows_kernels", 1)
         s.set_instance(inst, prec)
         if case.startswith("solve"):
             L64 = None
