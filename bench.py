@@ -477,6 +477,8 @@ def run_profile_case(case):
     inst = synth.make_config(CONFIG, seed=0)
     prec = pq.MIXED if case in ("mixed", "solvemix") else pq.FP64
     with pq.Solver(0) as s:
+        if case == "solve64":
+            s.set_option("rows_kernels", 1)  # the form the autotuner picks on this workload
         if case == "fp64":
             # no autotuning launches before the captured ones; the
             # row-flattened products, the form the autotuner picks here
