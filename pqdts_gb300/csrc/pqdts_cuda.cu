@@ -1036,6 +1036,27 @@ static int heuristic_tile(int R, int N, int nz = 1) {
   return 2;
 }
 
+// The FP32 Hessian row epilogue over hpart32's `parts` partials (row-
+// flattened where it applies); returns the number of p.Hp partials written.
+static int hvp_epilogue(Ctx& c, const float* p, const float* rs, const int8_t* ik, float* Hp, double* dpart,
+                        const double* pred, int parts) {
+  const int M = (int)c.h.M, N = (int)c.h.N;
+  const int RB = rows_per_block(N);
+  if (RB > 0 && c.rows_option != 0) {
+    const int threads = cdiv((int64_t)RB * N, 32) * 32;
+    k_hvp_epi32_rows<<<cdiv(M, RB), threads, 0, c.st>>>(c.hpart32.p, p, rs, c.maxr.p, rs ? 1 : 0,
+                                                         (float)(2.0 * c.h.gam), ik, M, N, RB, Hp, dpart, pred,
+                                                         parts);
+    post_launch(c);
+    return cdiv(M, RB);
+  }
+  const int tb = std::min(256, std::max(32, cdiv(N, 32) * 32));
+  k_hvp_epi32<<<M, tb, 0, c.st>>>(c.hpart32.p, p, rs, c.maxr.p, rs ? 1 : 0, (float)(2.0 * c.h.gam), ik, M, N, Hp,
+                                  dpart, pred, parts);
+  post_launch(c);
+  return M;
+}
+
 // Mixed precision Hessian product Hp = H p in FP32 with the tiled band
 // products (F.V then F^T.(2O)) and the row epilogue; p.Hp -> sc[SC_V2].
 // presplit: V's transposed split is already in place (k_lift_split32).
@@ -1056,14 +1077,9 @@ static void hvp32(Ctx& c, CGBufs<float>& b, const int8_t* ik, bool with_dot, con
     launch_band_gemm32(c, c.sched.trn_tile, c.tlo.p, c.tw.p, c.toff.p, c.tbval32.p, b.R2.p, M, N, 1.0f, c.hpart32.p,
                        pred, parts, 0, (int64_t)M * N, parts);
   }
-  const int tb = std::min(256, std::max(32, cdiv(N, 32) * 32));
-  // (one block per row: a grid-completion counter over M blocks costs more
-  // than the separate reduction)
-  k_hvp_epi32<<<M, tb, 0, c.st>>>(c.hpart32.p, b.p.p, c.fullspace ? nullptr : b.rs.p, c.maxr.p, c.fullspace ? 0 : 1,
-                                  (float)(2.0 * c.h.gam), ik, M, N, b.Hp.p, with_dot ? c.part.p : nullptr, pred,
-                                  parts);
-  post_launch(c);
-  if (with_dot) reduce_to(c, c.part.p, M, c.sc.p + SC_V2, 1, false, 0.0, pred);
+  const int nparts = hvp_epilogue(c, b.p.p, c.fullspace ? nullptr : b.rs.p, ik, b.Hp.p, with_dot ? c.part.p : nullptr,
+                                  pred, parts);
+  if (with_dot) reduce_to(c, c.part.p, nparts, c.sc.p + SC_V2, 1, false, 0.0, pred);
 }
 
 // A chunk of CG iterations captured as a CUDA graph (on first use of its
@@ -1870,11 +1886,7 @@ static Schedule heuristic_schedule(const HostProblem& h) {
 // The Hessian row epilogue over `parts` partials (full space, no mask), as
 // the CG runs it after the transposed product: part of that product's cost.
 static void tune_epilogue(Ctx& c, int parts) {
-  const int M = (int)c.h.M, N = (int)c.h.N;
-  const int tb = std::min(256, std::max(32, cdiv(N, 32) * 32));
-  k_hvp_epi32<<<M, tb, 0, c.st>>>(c.hpart32.p, c.cg32.p.p, nullptr, c.maxr.p, 0, (float)(2.0 * c.h.gam), nullptr, M, N,
-                                  c.cg32.Hp.p, c.part.p, nullptr, parts);
-  post_launch(c);
+  hvp_epilogue(c, c.cg32.p.p, nullptr, nullptr, c.cg32.Hp.p, c.part.p, nullptr, parts);
 }
 
 static void tune_schedule(Ctx& c, Schedule& s) {
