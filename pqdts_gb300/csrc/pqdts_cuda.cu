@@ -46,6 +46,7 @@ constexpr int kMaxCG = 50;                 // do j = 1, 50 (2036)
 constexpr int kMaxLS = 100;                // do i = 1, 100 (374, 420, 466)
 constexpr int kBatchLS = 8;                // step lengths evaluated per sweep
 constexpr int kElemGrid = 152 * 8;         // elementwise grids: 8 blocks per SM
+constexpr size_t kCondatSmemMax = 200u * 1024u;  // Condat's rows staged in shared memory up to this size
 
 struct Err : std::runtime_error {
   int code;
@@ -478,6 +479,7 @@ static void setup_device(Ctx& c) {
   }
   c.cg64.alloc(MN, M, D * N);
   c.sqd.alloc(M);
+  CK(cudaFuncSetAttribute(k_condat_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCondatSmemMax));
   c.counters.alloc(4);
   CK(cudaMemsetAsync(c.counters.p, 0, 4 * sizeof(unsigned), c.st));
   c.exact = (c.precision == PQDTS_FP64);
@@ -1327,8 +1329,13 @@ static void project_rows(Ctx& c, const double* X, const double* S, const double*
   const int M = (int)c.h.M, N = (int)c.h.N;
   const int64_t MN = (int64_t)M * N;
   if (c.exact) {
-    require(c.aux.p, "aux");
-    k_condat<<<dim3(cdiv(M, kRowThreads), B), kRowThreads, 0, c.st>>>(X, S, alphas, out, c.aux.p, MN, M, N);
+    const size_t smem = (size_t)2 * 33 * N * sizeof(double);
+    if (smem <= kCondatSmemMax) {
+      k_condat_smem<<<dim3(cdiv(M, 32), B), 32, smem, c.st>>>(X, S, alphas, out, MN, M, N);
+    } else {
+      require(c.aux.p, "aux");
+      k_condat<<<dim3(cdiv(M, kRowThreads), B), kRowThreads, 0, c.st>>>(X, S, alphas, out, c.aux.p, MN, M, N);
+    }
   } else {
     k_simplex<<<dim3(cdiv((int64_t)M * 32, 128), B), 128, 0, c.st>>>(X, S, alphas, out, MN, M, N);
   }
