@@ -766,9 +766,9 @@ static void op_dL(Ctx& c) {
 static void dot_dev(Ctx& c, const double* a, const double* b, double* out, const double* pred = nullptr) {
   const int M = (int)c.h.M, N = (int)c.h.N;
   if (c.exact) {
-    k_colchain<0><<<dim3(cdiv(N, 32), 1), 256, 0, c.st>>>(a, b, 0, M, N, 0.0, c.colbuf.p, nullptr, pred);
-    post_launch(c);
-    k_seqsum<<<1, 32, 0, c.st>>>(c.colbuf.p, N, nullptr, out, 1, pred);
+    // column chains, then (last block) their ascending sum into out
+    k_colchain<0><<<dim3(cdiv(N, 32), 1), 256, 0, c.st>>>(a, b, 0, M, N, 0.0, c.colbuf.p, nullptr, pred, out, 1,
+                                                          c.counters.p + 2);
     post_launch(c);
     return;
   }
@@ -784,9 +784,8 @@ static void dot_dev(Ctx& c, const double* a, const double* b, double* out, const
 static void dot2_exact(Ctx& c, const double* a, const double* b, double* out_ab, int ostride,
                        const double* pred) {
   const int M = (int)c.h.M, N = (int)c.h.N;
-  k_colchain<2><<<dim3(cdiv(N, 32), 1), 256, 0, c.st>>>(a, b, 0, M, N, 0.0, c.colbuf.p, c.colbuf.p + N, pred);
-  post_launch(c);
-  k_seqsum<<<1, 32, 0, c.st>>>(c.colbuf.p, N, nullptr, out_ab, 2, pred, ostride);
+  k_colchain<2><<<dim3(cdiv(N, 32), 1), 256, 0, c.st>>>(a, b, 0, M, N, 0.0, c.colbuf.p, c.colbuf.p + N, pred,
+                                                        out_ab, ostride, c.counters.p + 3);
   post_launch(c);
 }
 
