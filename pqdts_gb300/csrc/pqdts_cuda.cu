@@ -531,7 +531,7 @@ static void need_problem(Ctx& c) {
 // ---------------------------------------------------------------------------
 static void rebuild(Ctx& c, double* X, int B = 1) {
   const int M = (int)c.h.M, N = (int)c.h.N;
-  k_rebuild<<<dim3(cdiv(M, kRowThreads), B), kRowThreads, 0, c.st>>>(X, (int64_t)M * N, c.maxr.p, M, N);
+  k_rebuild_t<<<dim3(cdiv(M, 32), B), kTileThreads, 0, c.st>>>(X, (int64_t)M * N, c.maxr.p, M, N);
   post_launch(c);
 }
 
@@ -1348,9 +1348,9 @@ static void eval_candidates(Ctx& c, const double* al, int B, bool stage2, double
   const int64_t MN = (int64_t)M * N;
   CK(cudaMemcpyAsync(c.alphas.p, al, B * sizeof(double), cudaMemcpyHostToDevice, c.st));
   if (stage2) {
-    const int gb = cdiv(M, kRowThreads);
+    const int gb = cdiv(M, 32);  // 32-row tiles
     Scope s(c.timers, "doproj2");
-    k_cand_proj2<<<dim3(gb, B), kRowThreads, 0, c.st>>>(c.X.p, c.sn64.p, c.alphas.p, c.Xc.p, MN, c.maxr.p, M, N, 1,
+    k_cand_proj2_t<<<dim3(gb, B), kTileThreads, 0, c.st>>>(c.X.p, c.sn64.p, c.alphas.p, c.Xc.p, MN, c.maxr.p, M, N, 1,
                                                          c.part2.p);
     post_launch(c);
     reduce_to(c, c.part2.p, gb, c.lsout.p + 2 * kBatchLS, B, true, 0.0);
@@ -1472,8 +1472,8 @@ static void line_search_mixed(Ctx& c, bool stage2, double& alpha, double& dlalph
   auto screen = [&](const double* qa, int nb, double* dL, double* xmin) {
     CK(cudaMemcpyAsync(c.alphas.p, qa, nb * sizeof(double), cudaMemcpyHostToDevice, c.st));
     if (stage2) {
-      const int gb = cdiv(M, kRowThreads);
-      k_cand_proj2<<<dim3(gb, nb), kRowThreads, 0, c.st>>>(c.X.p, c.sn64.p, c.alphas.p, c.Xc.p, MN, c.maxr.p, M, N, 1,
+      const int gb = cdiv(M, 32);  // 32-row tiles
+      k_cand_proj2_t<<<dim3(gb, nb), kTileThreads, 0, c.st>>>(c.X.p, c.sn64.p, c.alphas.p, c.Xc.p, MN, c.maxr.p, M, N, 1,
                                                             c.part2.p);
       post_launch(c);
       reduce_to(c, c.part2.p, gb, c.lsout.p + 2 * kBatchLS, nb, true, 0.0);
@@ -1568,8 +1568,8 @@ static double op_conv(Ctx& c, bool tprint, bool with_extra = false) {
   op_dL(c);
   DBuf<double> lam;
   if (tprint && c.verbose) lam.alloc(M);
-  k_conv_rows<<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(c.X.p, c.G.p, M, N, c.part.p,
-                                                              (tprint && c.verbose) ? lam.p : nullptr);
+  k_conv_rows_t<<<cdiv(M, 32), kTileThreads, 0, c.st>>>(c.X.p, c.G.p, M, N, c.part.p,
+                                                        (tprint && c.verbose) ? lam.p : nullptr);
   post_launch(c);
   if (c.exact) {
     k_seqsum<<<1, 32, 0, c.st>>>(c.part.p, M, nullptr, c.sc.p + SC_TMP, 1, nullptr);
@@ -1616,7 +1616,7 @@ static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
   const int g = elem_grid(MN);
   if (mode == 1) {
     c.fullspace = false;
-    k_stage2_start<<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(c.X.p, c.maxr.p, M, N, 0);
+    k_stage2_start_t<<<cdiv(M, 32), kTileThreads, 0, c.st>>>(c.X.p, c.maxr.p, M, N, 0);
     post_launch(c);
     touch_x(c);
     op_dL(c);
@@ -1626,7 +1626,7 @@ static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
   } else {
     c.fullspace = (oiter == 1);
     if (!c.fullspace) {
-      k_stage2_start<<<cdiv(M, kRowThreads), kRowThreads, 0, c.st>>>(c.X.p, c.maxr.p, M, N, 1);
+      k_stage2_start_t<<<cdiv(M, 32), kTileThreads, 0, c.st>>>(c.X.p, c.maxr.p, M, N, 1);
       post_launch(c);
       if (c.exact) {
         touch_x(c);
@@ -1694,8 +1694,8 @@ static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
     touch_x(c);
   } else {
     Scope s(c.timers, "doproj2");
-    const int gb = cdiv(M, kRowThreads);
-    k_cand_proj2<<<dim3(gb, 1), kRowThreads, 0, c.st>>>(c.X.p, nullptr, nullptr, c.X.p, MN, c.maxr.p, M, N, 0,
+    const int gb = cdiv(M, 32);  // 32-row tiles
+    k_cand_proj2_t<<<dim3(gb, 1), kTileThreads, 0, c.st>>>(c.X.p, nullptr, nullptr, c.X.p, MN, c.maxr.p, M, N, 0,
                                                          c.part2.p);
     post_launch(c);
     touch_x(c);
@@ -2444,8 +2444,8 @@ int pqdts_cuda_doproj2(pqdts_ctx* c, double* xmin) {
   return guarded(c, [&] {
     pqdts::need_problem(*c);
     const int M = (int)c->h.M, N = (int)c->h.N;
-    const int gb = pqdts::cdiv(M, pqdts::kRowThreads);
-    pqdts::k_cand_proj2<<<dim3(gb, 1), pqdts::kRowThreads, 0, c->st>>>(c->X.p, nullptr, nullptr, c->X.p,
+    const int gb = pqdts::cdiv(M, 32);  // 32-row tiles
+    pqdts::k_cand_proj2_t<<<dim3(gb, 1), pqdts::kTileThreads, 0, c->st>>>(c->X.p, nullptr, nullptr, c->X.p,
                                                                          (int64_t)M * N, c->maxr.p, M, N, 0,
                                                                          c->part2.p);
     pqdts::post_launch(*c);
