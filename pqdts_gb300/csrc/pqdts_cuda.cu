@@ -612,7 +612,7 @@ static void objective_stack(Ctx& c, const double* Xs, int B) {
   require(c.Rst.p, "Rst");
   if (B < 1 || B > kBatchLS) throw Err(PQDTS_E_STATE, "internal: candidate batch out of range");
   launch_fwd<double, 3>(c, c.fval.p, Xs, (int64_t)M * N, c.P.p, c.Rst.p, B, nullptr);
-  k_rowchain_resid<<<dim3(cdiv(D, kRowThreads), B), kRowThreads, 0, c.st>>>(c.Rst.p, c.flo.p, D, N, 1.0, c.srow.p);
+  k_rowchain_resid_t<<<dim3(cdiv(D, 32), B), kTileThreads, 0, c.st>>>(c.Rst.p, c.flo.p, D, N, 1.0, c.srow.p);
   post_launch(c);
   objective_combine(c, Xs, B);
 }
@@ -651,7 +651,7 @@ static double op_L(Ctx& c) {
   if (c.L_ver == c.xver) return c.L_cache;
   ensure_R(c);
   const int D = (int)c.h.D, N = (int)c.h.N;
-  k_rowchain_resid<<<dim3(cdiv(D, kRowThreads), 1), kRowThreads, 0, c.st>>>(c.R.p, c.flo.p, D, N, 0.5, c.srow.p);
+  k_rowchain_resid_t<<<dim3(cdiv(D, 32), 1), kTileThreads, 0, c.st>>>(c.R.p, c.flo.p, D, N, 0.5, c.srow.p);
   post_launch(c);
   objective_combine(c, c.X.p, 1);
   double L;
