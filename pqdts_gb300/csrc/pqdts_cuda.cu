@@ -1188,10 +1188,20 @@ static void cg_solve32(Ctx& c, double bdfac) {
   const bool tc = c.sched.tc != 0;
   auto iteration = [&](bool first) {
     if (tc) {
-      // p update, lift and the first product's operand split in one pass
-      k_lift_split32<<<cdiv(M, 32), 256, 0, c.st>>>(first ? nullptr : c.sc.p, first ? 0 : 1, c.fullspace ? 0 : 1, M,
-                                                    N, b.p.p, b.z.p, c.maxr.p, b.rs.p, c.tc_mp, c.vt_hi.p,
-                                                    c.vt_lo.p);
+      // p update (and reduced space: row sums), then the first product's
+      // operand split with BF's lift applied on the fly (no row-major V)
+      if (c.fullspace) {
+        if (!first) {
+          k_cg_pupdate<float><<<g, 256, 0, c.st>>>(c.sc.p, MN, b.p.p, b.z.p);
+          post_launch(c);
+        }
+      } else {
+        k_cg_lift32<<<lift_blocks, 256, 0, c.st>>>(first ? nullptr : c.sc.p, first ? 0 : 1, M, N, b.p.p, b.z.p,
+                                                   c.maxr.p, nullptr, b.rs.p);
+        post_launch(c);
+      }
+      k_split_t<<<dim3(cdiv(M, 32), cdiv(N, 32)), dim3(32, 8), 0, c.st>>>(
+          b.p.p, M, N, c.tc_mp, c.vt_hi.p, c.vt_lo.p, c.sc.p, c.fullspace ? nullptr : c.maxr.p, b.rs.p);
       post_launch(c);
     } else if (c.fullspace) {
       if (!first) {

@@ -573,89 +573,23 @@ __global__ void k_finish_t(const float* __restrict__ part, int parts, int R, int
   }
 }
 
-// Mixed CG with tensor-core products, the start of an iteration in one
-// pass: p = beta p + z (do_update), in the reduced space BF's lift
-// (V = p, V(i,maxr) = -(sum(p(i,:)) - p(i,maxr)), rs(i) = that rest sum;
-// FP32 tree sums), and V's transposed split hi/lo for the first product.
-// A block takes 32 rows: warps update and sum rows, then 32-column tiles are
-// staged in shared memory and written transposed (32 consecutive rows per
-// column: coalesced).
-__global__ void __launch_bounds__(256) k_lift_split32(const double* __restrict__ sc, int do_update, int reduced,
-                                                      int M, int N, float* __restrict__ p,
-                                                      const float* __restrict__ z, const int32_t* __restrict__ maxr,
-                                                      float* __restrict__ rs, int64_t ld,
-                                                      __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
-  if (sc != nullptr && sc[SC_DONE] != 0.0) return;  // CG already converged
-  __shared__ float t[32][33];
-  __shared__ float s_rest[32];
-  __shared__ int s_m[32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int i0 = blockIdx.x * 32;
-  const float beta = do_update ? (float)sc[SC_V2] : 0.f;  // beta, left there by the previous step
-  for (int r = warp; r < 32; r += nw) {
-    const int i = i0 + r;
-    int m = -1;
-    float rest = 0.f;
-    if (i < M && (do_update || reduced)) {
-      float* pr = p + (int64_t)i * N;
-      const float* zr = z + (int64_t)i * N;
-      float sum = 0.f;
-      for (int n = lane; n < N; n += 32) {
-        float pv = pr[n];
-        if (do_update) {
-          pv = fmaf(beta, pv, zr[n]);
-          pr[n] = pv;
-        }
-        sum += pv;
-      }
-      if (reduced) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-        __syncwarp();
-        m = min(max(maxr[i], 0), N - 1);
-        rest = sum - pr[m];
-        if (lane == 0) rs[i] = rest;
-      }
-    }
-    if (lane == 0) {
-      s_m[r] = m;
-      s_rest[r] = rest;
-    }
-  }
-  __syncthreads();
-  for (int n0 = 0; n0 < N; n0 += 32) {
-    for (int r = warp; r < 32; r += nw) {
-      const int i = i0 + r, n = n0 + lane;
-      float v = 0.f;
-      if (i < M && n < N) {
-        v = p[(int64_t)i * N + n];
-        if (n == s_m[r]) v = -s_rest[r];
-      }
-      t[r][lane] = v;
-    }
-    __syncthreads();
-    for (int r = warp; r < 32; r += nw) {
-      const int n = n0 + r, i = i0 + lane;
-      if (n < N && i < M) {
-        const float x = t[lane][r];
-        const __nv_bfloat16 h = __float2bfloat16_rn(x);
-        hi[(int64_t)n * ld + i] = h;
-        lo[(int64_t)n * ld + i] = __float2bfloat16_rn(x - __bfloat162float(h));
-      }
-    }
-    __syncthreads();
-  }
-}
-
 // V (M x N row-major FP32) -> V^T split: hi[n * ld + i], lo[n * ld + i].
+// With maxr != null V is BF's reduced-space lift of the input (260-267):
+// entry (i, maxr[i]) is replaced by -rs[i].
 __global__ void k_split_t(const float* __restrict__ V, int M, int N, int64_t ld, __nv_bfloat16* __restrict__ hi,
-                          __nv_bfloat16* __restrict__ lo, const double* __restrict__ pred) {
+                          __nv_bfloat16* __restrict__ lo, const double* __restrict__ pred,
+                          const int32_t* __restrict__ maxr = nullptr, const float* __restrict__ rs = nullptr) {
   if (pred != nullptr && pred[6] != 0.0) return;
   __shared__ float t[32][33];
   const int i0 = blockIdx.x * 32, n0 = blockIdx.y * 32;
   for (int rr = threadIdx.y; rr < 32; rr += blockDim.y) {
     const int i = i0 + rr, n = n0 + threadIdx.x;
-    t[rr][threadIdx.x] = (i < M && n < N) ? V[(int64_t)i * N + n] : 0.f;
+    float v = 0.f;
+    if (i < M && n < N) {
+      v = V[(int64_t)i * N + n];
+      if (maxr != nullptr && n == min(max(maxr[i], 0), N - 1)) v = -rs[i];
+    }
+    t[rr][threadIdx.x] = v;
   }
   __syncthreads();
   for (int rr = threadIdx.y; rr < 32; rr += blockDim.y) {
