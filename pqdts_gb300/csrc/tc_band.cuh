@@ -79,6 +79,11 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
+// Fetch a TMA descriptor ahead of its first use (overlaps the set-up).
+__device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap* map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(map) : "memory");
+}
+
 __device__ __forceinline__ void tc_alloc(uint32_t* dst, uint32_t ncols) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
                : "memory");
@@ -187,6 +192,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t stage_bytes = 2u * a_bytes + 2u * b_bytes;
 
   if (threadIdx.x == 0) {
+    tma_prefetch_desc(&mA_hi);
+    tma_prefetch_desc(&mA_lo);
+    tma_prefetch_desc(&mB_hi);
+    tma_prefetch_desc(&mB_lo);
     for (int i = 0; i < stages; ++i) {
       mbar_init(&bar_full[i], 1);
       mbar_init(&bar_empty[i], 1);
@@ -374,6 +383,10 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
   const uint32_t ncols = tc_tmem_cols(BN);  // per accumulator
 
   if (threadIdx.x == 0) {
+    tma_prefetch_desc(&mA_hi);
+    tma_prefetch_desc(&mA_lo);
+    tma_prefetch_desc(&mB_hi);
+    tma_prefetch_desc(&mB_lo);
     for (int i = 0; i < stages; ++i) {
       mbar_init(&bar_full[i], 1);
       mbar_init(&bar_empty[i], 1);
