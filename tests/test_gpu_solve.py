@@ -180,3 +180,26 @@ def test_row_flattened_products_bitwise(built, mid, rows):
         X = s.get_x()
     Xo, so = Oracle.from_instance(mid).solve(mode=2, maxiter=200, eps=mid.eps)
     assert st["L"] == so["L"] and st["cg"] == so["cg"] and np.array_equal(X, Xo)
+
+
+@pytest.mark.parametrize("shape", [(2, 1, 3), (3, 2, 1), (5, 33, 4), (40, 3, 2)])
+def test_tiny_shapes(built, shape):
+    """Degenerate sizes: one outcome (N = 1), one probe (D = 1), M = 2, N
+    just above a warp: the FP64 trajectory is the oracle's bit for bit and the
+    mixed solve (tensor-core products) stays feasible."""
+    import pqdts_gb300 as pq
+    from oracle.oracle import Oracle
+    from pqdts_gb300 import synth
+
+    M, N, D = shape
+    inst = synth.make_instance(M=M, N=N, D=D, xmax=2.0 * M, eta=0.8, shots=10**4, gamma=1e-3, eps=1e-6, seed=2)
+    X, st, _ = _solve_gpu(inst, maxiter=50)
+    Xo, so = Oracle.from_instance(inst).solve(mode=2, maxiter=50, eps=inst.eps)
+    assert st["L"] == so["L"] and st["cg"] == so["cg"] and np.array_equal(X, Xo)
+    with pq.Solver(0) as s:
+        s.set_option("tensor_cores", 1)
+        s.set_instance(inst, pq.MIXED)
+        sm = s.solve(mode=2, maxiter=50, eps=inst.eps)
+        Xm = s.get_x()
+    assert np.isfinite(sm["L"])
+    _feasible(Xm)
