@@ -68,6 +68,11 @@ int pqdts_cuda_kernel_launches(pqdts_ctx* ctx, int64_t* count);
  *              form (one CTA per output tile, or persistent with
  *              double-buffered accumulators); "tc_splits1" -1 (autotuned) or
  *              1..8: K segments of the tensor-core F.V product.
+ *   "df_products" -1 (default, auto) / 1: the mixed path's gradient F^T.R
+ *              and its objective checks (residual F.X - P) in double-FP32
+ *              (pairs of FP32 numbers, ~2^-46 relative to the sum of the
+ *              terms' magnitudes) on the CUDA cores; 0: native FP64.  Takes
+ *              effect at the next set_problem.
  * Unknown names return PQDTS_E_ARG. */
 int pqdts_cuda_set_option(pqdts_ctx* ctx, const char* name, int64_t value);
 /* Reads an option above or a field of the schedule in use:
@@ -79,7 +84,8 @@ int pqdts_cuda_set_option(pqdts_ctx* ctx, const char* name, int64_t value);
  * "sched.fwd_rows", "sched.trans_rows" (row-flattened FP64 products in use),
  * "sched.tc_splits" (K segments of their F^T product), "sched.tc_splits1"
  * (of their F.V product), "sched.tc_persistent" (kernel form),
- * "graphs.captured" (graphs held). */
+ * "sched.df_fwd", "sched.df_trans" (double-FP32 residual / gradient
+ * products in use), "graphs.captured" (graphs held). */
 int pqdts_cuda_get_option(pqdts_ctx* ctx, const char* name, int64_t* value);
 /* verbose = 1 prints the reference's stdout lines (iter, newton-pcg, line
  * search, positivity constraints) exactly as rank 0 of pqdts_omp.x. */

@@ -335,6 +335,12 @@ struct pqdts_ctx {
   pqdts::DBuf<float> r0_32, d32, fdx32, hpart32;
   pqdts::DBuf<double> Gf;  // mixed path: full-space gradient of X (version Gf_ver)
   int64_t Gf_ver = -1;
+  // mixed path: double-FP32 banded products for the gradient and the FP64
+  // objective checks (option -1 auto = on, 0 native FP64, 1 on): F and F^T
+  // values, and the split X and R operands, as (hi, lo) pairs
+  pqdts::DBuf<float2> fdf, tdf, xdf, rdf;
+  int df_option = -1;
+  bool df_fwd = false, df_trans = false;
   bool exact = true;  // FP64: every reduction in the oracle's order
   pqdts::DBuf<int> ipart;
   pqdts::DBuf<long long> icount;
@@ -435,6 +441,12 @@ static void read_back(Ctx& c, const double* dev, int count) {
 // ---------------------------------------------------------------------------
 // Problem upload and buffer allocation.
 // ---------------------------------------------------------------------------
+// (hi, lo) FP32 pair of an FP64 value, as k_split_df forms it on the device.
+static float2 split_df_host(double v) {
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
+
 static void setup_device(Ctx& c) {
   HostProblem& h = c.h;
   const int64_t M = h.M, N = h.N, D = h.D, MN = M * N;
@@ -471,11 +483,36 @@ static void setup_device(Ctx& c) {
     c.r0_32.alloc(D * N);
     c.d32.alloc((size_t)kBatchLS * MN);
     c.fdx32.alloc((size_t)kBatchLS * D * N);
+    c.df_fwd = c.df_option != 0;
+    c.df_trans = c.df_fwd && c.t_contiguous;
+    if (c.df_fwd) {
+      std::vector<float2> fd(h.fval.size());
+      for (size_t k = 0; k < fd.size(); ++k) fd[k] = split_df_host(h.fval[k]);
+      c.fdf.upload(fd.data(), fd.size(), c.st, &c.h2d);
+      c.xdf.alloc(MN);
+    } else {
+      c.fdf.release();
+      c.xdf.release();
+    }
+    if (c.df_trans) {
+      std::vector<float2> td(h.tval.size());
+      for (size_t k = 0; k < td.size(); ++k) td[k] = split_df_host(h.tval[k]);
+      c.tdf.upload(td.data(), td.size(), c.st, &c.h2d);
+      c.rdf.alloc(D * N);
+    } else {
+      c.tdf.release();
+      c.rdf.release();
+    }
     CK(cudaStreamSynchronize(c.st));  // host staging vectors go out of scope
   } else {
     c.fval32.release();
     c.tval32.release();
     c.tbval32.release();
+    c.fdf.release();
+    c.tdf.release();
+    c.xdf.release();
+    c.rdf.release();
+    c.df_fwd = c.df_trans = false;
   }
   c.cg64.alloc(MN, M, D * N);
   c.sqd.alloc(M);
@@ -607,11 +644,45 @@ static void launch_fwd(Ctx& c, const T* fv, const T* X, int64_t xstride, const d
   post_launch(c);
 }
 
+// Block shape of the double-FP32 products: RB rows x NC columns per block,
+// `chunks` column chunks (N > 1024 only).
+static void df_shape(int N, int& RB, int& NC, int& chunks) {
+  if (N > 1024) {
+    chunks = cdiv(N, 1024);
+    NC = cdiv(cdiv(N, chunks), 32) * 32;
+    RB = 1;
+  } else {
+    chunks = 1;
+    NC = N;
+    RB = N >= 32 ? rows_per_block(N) : std::min(32, 1024 / N);
+  }
+}
+
+// Residual of X (FP64, M x N) in double-FP32: MODE 0 R = 2*(F.X - P),
+// MODE 3 R = F.X - P.
+template <int MODE>
+static void fwd_df(Ctx& c, const double* X, double* R) {
+  const int N = (int)c.h.N, D = (int)c.h.D;
+  const int64_t MN = c.h.M * c.h.N;
+  require(c.xdf.p, "xdf");
+  k_split_df<<<elem_grid(MN), 256, 0, c.st>>>(X, MN, 1.0, c.xdf.p);
+  post_launch(c);
+  int RB, NC, chunks;
+  df_shape(N, RB, NC, chunks);
+  k_fwd_df<MODE><<<dim3(cdiv(D, RB), chunks), cdiv((int64_t)RB * NC, 32) * 32, 0, c.st>>>(bands_of(c), c.fdf.p, c.xdf.p,
+                                                                                          c.P.p, R, RB, NC);
+  post_launch(c);
+}
+
 static void objective_stack(Ctx& c, const double* Xs, int B) {
   const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
   require(c.Rst.p, "Rst");
   if (B < 1 || B > kBatchLS) throw Err(PQDTS_E_STATE, "internal: candidate batch out of range");
-  launch_fwd<double, 3>(c, c.fval.p, Xs, (int64_t)M * N, c.P.p, c.Rst.p, B, nullptr);
+  if (c.df_fwd) {
+    for (int b = 0; b < B; ++b) fwd_df<3>(c, Xs + (size_t)b * M * N, c.Rst.p + (size_t)b * D * N);
+  } else {
+    launch_fwd<double, 3>(c, c.fval.p, Xs, (int64_t)M * N, c.P.p, c.Rst.p, B, nullptr);
+  }
   k_rowchain_resid_t<<<dim3(cdiv(D, 32), B), kTileThreads, 0, c.st>>>(c.Rst.p, c.flo.p, D, N, 1.0, c.srow.p);
   post_launch(c);
   objective_combine(c, Xs, B);
@@ -639,7 +710,8 @@ static void rebuild_x(Ctx& c) {
 // for this version of X.
 static void ensure_R(Ctx& c) {
   if (c.R_ver == c.xver) return;
-  launch_fwd<double, 0>(c, c.fval.p, c.X.p, 0, c.P.p, c.R.p, 1, nullptr);
+  if (c.df_fwd) fwd_df<0>(c, c.X.p, c.R.p);
+  else launch_fwd<double, 0>(c, c.fval.p, c.X.p, 0, c.P.p, c.R.p, 1, nullptr);
   c.R_ver = c.xver;
 }
 
@@ -747,6 +819,23 @@ static void op_dL(Ctx& c) {
       k_reduced_from_full<<<M, std::min(256, std::max(32, cdiv(N, 32) * 32)), 0, c.st>>>(c.Gf.p, c.maxr.p, N, c.G.p);
       post_launch(c);
     }
+  } else if (c.df_trans) {
+    // mixed path, double-FP32: full-space gradient into Gf (and G), then
+    // the reduced one from it
+    ensure_R(c);
+    const int D = (int)c.h.D;
+    k_split_df<<<elem_grid((int64_t)D * N), 256, 0, c.st>>>(c.R.p, (int64_t)D * N, 1.0, c.rdf.p);
+    post_launch(c);
+    int RB, NC, chunks;
+    df_shape(N, RB, NC, chunks);
+    k_trans_df<<<dim3(cdiv(M, RB), chunks), cdiv((int64_t)RB * NC, 32) * 32, 0, c.st>>>(
+        bands_of(c), c.tdf.p, c.rdf.p, c.X.p, 2.0 * c.h.gam, RB, NC, c.fullspace ? c.G.p : nullptr, c.Gf.p);
+    post_launch(c);
+    if (!c.fullspace) {
+      k_reduced_from_full<<<M, std::min(256, std::max(32, cdiv(N, 32) * 32)), 0, c.st>>>(c.Gf.p, c.maxr.p, N, c.G.p);
+      post_launch(c);
+    }
+    c.Gf_ver = c.xver;
   } else {
     ensure_R(c);
     double* gf = (!c.exact && !c.fullspace) ? c.Gf.p : nullptr;
@@ -2580,6 +2669,9 @@ int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
     } else if (n == "tensor_cores") {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "tensor_cores must be -1, 0 or 1");
       c->tc_option = (int)value;
+    } else if (n == "df_products") {
+      if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "df_products must be -1, 0 or 1");
+      c->df_option = (int)value;
     } else {
       throw pqdts::Err(PQDTS_E_ARG, "unknown option " + n);
     }
@@ -2610,6 +2702,9 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     else if (n == "rows_kernels") *value = c->rows_option;
     else if (n == "tc_persistent") *value = c->tc_persistent_option;
     else if (n == "tensor_cores") *value = c->tc_option;
+    else if (n == "df_products") *value = c->df_option;
+    else if (n == "sched.df_fwd") *value = c->df_fwd;
+    else if (n == "sched.df_trans") *value = c->df_trans;
     else if (n == "graphs.captured") *value = (int64_t)c->graphs.size();
     else throw pqdts::Err(PQDTS_E_ARG, "unknown option " + n);
   });

@@ -200,3 +200,44 @@ def test_BF32_mixed_precision(built, cfg1, full):
     H64 = o.BF(V)
     err = np.max(np.abs(H32 - H64)) / np.max(np.abs(H64))
     assert err < 2e-5, err
+
+
+def _df_instances():
+    from pqdts_gb300 import synth
+
+    return {
+        # N > 1024: two column chunks per row block
+        "wide": synth.make_instance(M=40, N=1100, D=90, xmax=60.0, eta=0.8, shots=10**6, gamma=1e-3, eps=1e-6,
+                                    seed=7),
+    }
+
+
+@pytest.mark.parametrize("which", ["cfg1", "small", "mid", "empty_rows", "wide"])
+@pytest.mark.parametrize("full", [True, False])
+def test_L_dL_double_float(built, request, which, full):
+    """The mixed path's objective and gradient products in double-FP32
+    (pairs of FP32 numbers): ~2^-46 relative to the terms' magnitudes, so L
+    within 1e-12 relative and dL within 1e-11 of max|dL| of the FP64 oracle."""
+    import pqdts_gb300 as pq
+    from oracle.oracle import Oracle
+
+    inst = _df_instances()[which] if which == "wide" else request.getfixturevalue(which)
+    s = pq.Solver(0)
+    s.set_option("df_products", 1)
+    s.set_instance(inst, pq.MIXED)
+    assert s.get_option("sched.df_fwd") == 1 and s.get_option("sched.df_trans") == 1
+    o = Oracle.from_instance(inst)
+    X = _random_x(inst, 3)
+    m = None if full else _maxr(X)
+    s.set_space(full, m)
+    o.set_space(full, m)
+    s.set_x(X)
+    Lg = s.L()
+    Lo, _ = o.L(X)
+    assert abs(Lg - Lo) <= 1e-12 * abs(Lo), (Lg, Lo)
+    s.set_x(X)
+    G = s.dL()
+    Go, _ = o.dL(X)
+    err = np.max(np.abs(G - Go)) / np.max(np.abs(Go))
+    assert err < 1e-11, err
+    s.close()

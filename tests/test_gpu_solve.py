@@ -63,10 +63,19 @@ def test_mode1_matches_oracle(built, small):
 
 
 @pytest.mark.parametrize("which", ["cfg1", "small"])
-def test_mixed_precision_solve(built, request, which):
+@pytest.mark.parametrize("df", [1, 0])
+def test_mixed_precision_solve(built, request, which, df):
+    """df = 1: gradient and objective checks in double-FP32; 0: native FP64."""
+    import pqdts_gb300 as pq
+
     inst = request.getfixturevalue(which)
     X64, s64, _ = _solve_gpu(inst, 0, maxiter=2000, eps=1e-9)
-    X32, s32, _ = _solve_gpu(inst, 1, maxiter=2000, eps=1e-9)
+    with pq.Solver(0) as s:
+        s.set_option("df_products", df)
+        s.set_instance(inst, pq.MIXED)
+        assert s.get_option("sched.df_fwd") == df
+        s32 = s.solve(mode=2, maxiter=2000, eps=1e-9)
+        X32 = s.get_x()
     assert abs(s32["L"] - s64["L"]) <= MIXED_OBJ_REL * abs(s64["L"]), (s32, s64)
     # Pi at the same convergence: within 1e-4 max-abs (measured ~1e-5 on
     # configuration 1, ~1e-6 on the small instance)
