@@ -340,6 +340,7 @@ struct pqdts_ctx {
   // values, and the split X and R operands, as (hi, lo) pairs
   pqdts::DBuf<float2> fdf, tdf, xdf, rdf;
   int df_option = -1;
+  int df_rows = 0, df_kc = 0;  // launch shape of the double-FP32 products (0: the default)
   bool df_fwd = false, df_trans = false;
   bool exact = true;  // FP64: every reduction in the oracle's order
   pqdts::DBuf<int> ipart;
@@ -441,6 +442,40 @@ static void read_back(Ctx& c, const double* dev, int count) {
 // ---------------------------------------------------------------------------
 // Problem upload and buffer allocation.
 // ---------------------------------------------------------------------------
+// Launch shape of the double-FP32 products: N in `chunks` equal column
+// chunks of NC <= 256, RB rows per block (the most busy lanes with
+// RB*NC <= 1024 and RB <= rbmax <= 32, the most rows among equals: each
+// staged chunk of the operand serves RB rows), KC band terms per staged
+// chunk: 32 (two blocks of 1024 threads per SM), or 64 on request where its
+// double buffer fits in shared memory (measured slower on M=2000, N=200,
+// D=4000: fewer resident blocks).
+struct DfShape {
+  int RB, NC, chunks, KC;
+};
+constexpr int kDfSmemCap = 226 * 1024;  // 227 KB opt-in per block, less the kernels' static DfRows
+static size_t df_smem(int RB, int NC, int KC) { return (size_t)2 * df_stage_elems(RB, NC, KC) * sizeof(float2); }
+// the largest shared memory of a KC = 32 shape (NC + RB <= 260)
+constexpr size_t kDfSmem32 = (size_t)2 * df_stage_elems(4, 256, 32) * sizeof(float2);
+
+static DfShape df_shape(int N, int rbmax, int kc) {
+  DfShape sh;
+  sh.chunks = cdiv(N, 256);
+  sh.NC = cdiv(N, sh.chunks);
+  sh.RB = 1;
+  double best = 0.0;
+  const int rcap = rbmax > 0 ? std::min(rbmax, 32) : 32;
+  for (int rb = 1; rb <= rcap && rb * sh.NC <= 1024; ++rb) {
+    const int t = rb * sh.NC;
+    const double eff = (double)t / (32.0 * cdiv(t, 32));
+    if (eff >= best - 1e-12) {
+      best = std::max(best, eff);
+      sh.RB = rb;
+    }
+  }
+  sh.KC = (kc == 64 && df_smem(sh.RB, sh.NC, 64) <= (size_t)kDfSmemCap) ? 64 : 32;
+  return sh;
+}
+
 // (hi, lo) FP32 pair of an FP64 value, as k_split_df forms it on the device.
 static float2 split_df_host(double v) {
   const float h = (float)v;
@@ -486,6 +521,13 @@ static void setup_device(Ctx& c) {
     c.df_fwd = c.df_option != 0;
     c.df_trans = c.df_fwd && c.t_contiguous;
     if (c.df_fwd) {
+      // the same attribute values from every context, whatever its N
+      CK(cudaFuncSetAttribute(k_fwd_df<0, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDfSmem32));
+      CK(cudaFuncSetAttribute(k_fwd_df<3, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDfSmem32));
+      CK(cudaFuncSetAttribute(k_trans_df<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDfSmem32));
+      CK(cudaFuncSetAttribute(k_fwd_df<0, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDfSmemCap));
+      CK(cudaFuncSetAttribute(k_fwd_df<3, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDfSmemCap));
+      CK(cudaFuncSetAttribute(k_trans_df<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDfSmemCap));
       std::vector<float2> fd(h.fval.size());
       for (size_t k = 0; k < fd.size(); ++k) fd[k] = split_df_host(h.fval[k]);
       c.fdf.upload(fd.data(), fd.size(), c.st, &c.h2d);
@@ -644,19 +686,6 @@ static void launch_fwd(Ctx& c, const T* fv, const T* X, int64_t xstride, const d
   post_launch(c);
 }
 
-// Block shape of the double-FP32 products: RB rows x NC columns per block,
-// `chunks` column chunks (N > 1024 only).
-static void df_shape(int N, int& RB, int& NC, int& chunks) {
-  if (N > 1024) {
-    chunks = cdiv(N, 1024);
-    NC = cdiv(cdiv(N, chunks), 32) * 32;
-    RB = 1;
-  } else {
-    chunks = 1;
-    NC = N;
-    RB = N >= 32 ? rows_per_block(N) : std::min(32, 1024 / N);
-  }
-}
 
 // Residual of X (FP64, M x N) in double-FP32: MODE 0 R = 2*(F.X - P),
 // MODE 3 R = F.X - P.
@@ -667,10 +696,14 @@ static void fwd_df(Ctx& c, const double* X, double* R) {
   require(c.xdf.p, "xdf");
   k_split_df<<<elem_grid(MN), 256, 0, c.st>>>(X, MN, 1.0, c.xdf.p);
   post_launch(c);
-  int RB, NC, chunks;
-  df_shape(N, RB, NC, chunks);
-  k_fwd_df<MODE><<<dim3(cdiv(D, RB), chunks), cdiv((int64_t)RB * NC, 32) * 32, 0, c.st>>>(bands_of(c), c.fdf.p, c.xdf.p,
-                                                                                          c.P.p, R, RB, NC);
+  const DfShape sh = df_shape(N, c.df_rows, c.df_kc);
+  const dim3 grid(cdiv(D, sh.RB), sh.chunks);
+  const int threads = cdiv((int64_t)sh.RB * sh.NC, 32) * 32;
+  const size_t smem = df_smem(sh.RB, sh.NC, sh.KC);
+  if (sh.KC == 64)
+    k_fwd_df<MODE, 64><<<grid, threads, smem, c.st>>>(bands_of(c), c.fdf.p, c.xdf.p, c.P.p, R, sh.RB, sh.NC);
+  else
+    k_fwd_df<MODE, 32><<<grid, threads, smem, c.st>>>(bands_of(c), c.fdf.p, c.xdf.p, c.P.p, R, sh.RB, sh.NC);
   post_launch(c);
 }
 
@@ -826,10 +859,17 @@ static void op_dL(Ctx& c) {
     const int D = (int)c.h.D;
     k_split_df<<<elem_grid((int64_t)D * N), 256, 0, c.st>>>(c.R.p, (int64_t)D * N, 1.0, c.rdf.p);
     post_launch(c);
-    int RB, NC, chunks;
-    df_shape(N, RB, NC, chunks);
-    k_trans_df<<<dim3(cdiv(M, RB), chunks), cdiv((int64_t)RB * NC, 32) * 32, 0, c.st>>>(
-        bands_of(c), c.tdf.p, c.rdf.p, c.X.p, 2.0 * c.h.gam, RB, NC, c.fullspace ? c.G.p : nullptr, c.Gf.p);
+    const DfShape sh = df_shape(N, c.df_rows, c.df_kc);
+    const dim3 grid(cdiv(M, sh.RB), sh.chunks);
+    const int threads = cdiv((int64_t)sh.RB * sh.NC, 32) * 32;
+    const size_t smem = df_smem(sh.RB, sh.NC, sh.KC);
+    double* g = c.fullspace ? c.G.p : nullptr;
+    if (sh.KC == 64)
+      k_trans_df<64><<<grid, threads, smem, c.st>>>(bands_of(c), c.tdf.p, c.rdf.p, c.X.p, 2.0 * c.h.gam, sh.RB, sh.NC,
+                                                    g, c.Gf.p);
+    else
+      k_trans_df<32><<<grid, threads, smem, c.st>>>(bands_of(c), c.tdf.p, c.rdf.p, c.X.p, 2.0 * c.h.gam, sh.RB, sh.NC,
+                                                    g, c.Gf.p);
     post_launch(c);
     if (!c.fullspace) {
       k_reduced_from_full<<<M, std::min(256, std::max(32, cdiv(N, 32) * 32)), 0, c.st>>>(c.Gf.p, c.maxr.p, N, c.G.p);
@@ -2672,6 +2712,12 @@ int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
     } else if (n == "df_products") {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "df_products must be -1, 0 or 1");
       c->df_option = (int)value;
+    } else if (n == "df_rows") {
+      if (value < 0 || value > 32) throw pqdts::Err(PQDTS_E_ARG, "df_rows must be 0..32");
+      c->df_rows = (int)value;
+    } else if (n == "df_kc") {
+      if (value != 0 && value != 32 && value != 64) throw pqdts::Err(PQDTS_E_ARG, "df_kc must be 0, 32 or 64");
+      c->df_kc = (int)value;
     } else {
       throw pqdts::Err(PQDTS_E_ARG, "unknown option " + n);
     }
@@ -2703,6 +2749,8 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     else if (n == "tc_persistent") *value = c->tc_persistent_option;
     else if (n == "tensor_cores") *value = c->tc_option;
     else if (n == "df_products") *value = c->df_option;
+    else if (n == "df_rows") *value = c->df_rows;
+    else if (n == "df_kc") *value = c->df_kc;
     else if (n == "sched.df_fwd") *value = c->df_fwd;
     else if (n == "sched.df_trans") *value = c->df_trans;
     else if (n == "graphs.captured") *value = (int64_t)c->graphs.size();
