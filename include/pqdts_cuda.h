@@ -72,10 +72,9 @@ int pqdts_cuda_kernel_launches(pqdts_ctx* ctx, int64_t* count);
  *              and its objective checks (residual F.X - P) in double-FP32
  *              (pairs of FP32 numbers, ~2^-46 relative to the sum of the
  *              terms' magnitudes) on the CUDA cores; 0: native FP64.  Takes
- *              effect at the next set_problem.  "df_rows" 0 (default) or
- *              1..32: at most that many band rows per block of those
- *              products; "df_kc" 0 (default, 32) / 32 / 64: band terms per
- *              shared-memory stage.
+ *              effect at the next set_problem.  "df_rows" 0 (default,
+ *              chosen by size) / 2 / 4 / 8: band rows per block of those
+ *              products (each thread accumulates that many outputs).
  * Unknown names return PQDTS_E_ARG. */
 int pqdts_cuda_set_option(pqdts_ctx* ctx, const char* name, int64_t value);
 /* Reads an option above or a field of the schedule in use:

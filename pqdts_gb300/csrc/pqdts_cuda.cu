@@ -340,7 +340,7 @@ struct pqdts_ctx {
   // values, and the split X and R operands, as (hi, lo) pairs
   pqdts::DBuf<float2> fdf, tdf, xdf, rdf;
   int df_option = -1;
-  int df_rows = 0, df_kc = 0;  // launch shape of the double-FP32 products (0: the default)
+  int df_rows = 0;  // band rows per block of the double-FP32 products (0: chosen by size)
   bool df_fwd = false, df_trans = false;
   bool exact = true;  // FP64: every reduction in the oracle's order
   pqdts::DBuf<int> ipart;
@@ -442,39 +442,31 @@ static void read_back(Ctx& c, const double* dev, int count) {
 // ---------------------------------------------------------------------------
 // Problem upload and buffer allocation.
 // ---------------------------------------------------------------------------
-// Launch shape of the double-FP32 products: N in `chunks` equal column
-// chunks of NC <= 256, RB rows per block (the most busy lanes with
-// RB*NC <= 1024 and RB <= rbmax <= 32, the most rows among equals: each
-// staged chunk of the operand serves RB rows), KC band terms per staged
-// chunk: 32 (two blocks of 1024 threads per SM), or 64 on request where its
-// double buffer fits in shared memory (measured slower on M=2000, N=200,
-// D=4000: fewer resident blocks).
-struct DfShape {
-  int RB, NC, chunks, KC;
-};
-constexpr int kDfSmemCap = 226 * 1024;  // 227 KB opt-in per block, less the kernels' static DfRows
-static size_t df_smem(int RB, int NC, int KC) { return (size_t)2 * df_stage_elems(RB, NC, KC) * sizeof(float2); }
-// the largest shared memory of a KC = 32 shape (NC + RB <= 260)
-constexpr size_t kDfSmem32 = (size_t)2 * df_stage_elems(4, 256, 32) * sizeof(float2);
-
-static DfShape df_shape(int N, int rbmax, int kc) {
-  DfShape sh;
-  sh.chunks = cdiv(N, 256);
-  sh.NC = cdiv(N, sh.chunks);
-  sh.RB = 1;
-  double best = 0.0;
-  const int rcap = rbmax > 0 ? std::min(rbmax, 32) : 32;
-  for (int rb = 1; rb <= rcap && rb * sh.NC <= 1024; ++rb) {
-    const int t = rb * sh.NC;
-    const double eff = (double)t / (32.0 * cdiv(t, 32));
-    if (eff >= best - 1e-12) {
-      best = std::max(best, eff);
-      sh.RB = rb;
-    }
-  }
-  sh.KC = (kc == 64 && df_smem(sh.RB, sh.NC, 64) <= (size_t)kDfSmemCap) ? 64 : 32;
-  return sh;
+// Band rows per block of the double-FP32 products: the most of 8, 4, 2
+// that still gives >= 40 warps per SM to cover the operand loads' latency
+// (measured: M=2000, N=200, D=4000 runs best at 4 rows for F.X and 2 for
+// F^T.R; M=10^4, N=10^3, D=2*10^4 at 8); rbopt > 0: that, as 2/4/8.
+static int df_rows_per_block(int64_t rows, int N, int rbopt, int sms) {
+  if (rbopt > 0) return rbopt >= 8 ? 8 : (rbopt >= 4 ? 4 : 2);
+  const int64_t wpr = cdiv(N, 32);
+  for (int rb : {8, 4})
+    if ((rows + rb - 1) / rb * wpr >= (int64_t)40 * sms) return rb;
+  return 2;
 }
+
+template <int MODE>
+static void launch_fwd_df(Ctx& c, double* R) {
+  const int N = (int)c.h.N, D = (int)c.h.D;
+  const int rb = df_rows_per_block(D, N, c.df_rows, c.num_sms);
+  const dim3 grid(cdiv(D, rb), cdiv(N, 32 * kDfColWarps));
+  const int threads = 32 * std::min(kDfColWarps, cdiv(N, 32));
+  DevBands bd = bands_of(c);
+  if (rb == 8) k_fwd_df<MODE, 8><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R);
+  else if (rb == 4) k_fwd_df<MODE, 4><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R);
+  else k_fwd_df<MODE, 2><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R);
+  post_launch(c);
+}
+
 
 // (hi, lo) FP32 pair of an FP64 value, as k_split_df forms it on the device.
 static float2 split_df_host(double v) {
@@ -520,14 +512,8 @@ static void setup_device(Ctx& c) {
     c.fdx32.alloc((size_t)kBatchLS * D * N);
     c.df_fwd = c.df_option != 0;
     c.df_trans = c.df_fwd && c.t_contiguous;
+    CK(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, c.device));
     if (c.df_fwd) {
-      // the same attribute values from every context, whatever its N
-      CK(cudaFuncSetAttribute(k_fwd_df<0, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDfSmem32));
-      CK(cudaFuncSetAttribute(k_fwd_df<3, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDfSmem32));
-      CK(cudaFuncSetAttribute(k_trans_df<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDfSmem32));
-      CK(cudaFuncSetAttribute(k_fwd_df<0, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDfSmemCap));
-      CK(cudaFuncSetAttribute(k_fwd_df<3, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDfSmemCap));
-      CK(cudaFuncSetAttribute(k_trans_df<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDfSmemCap));
       std::vector<float2> fd(h.fval.size());
       for (size_t k = 0; k < fd.size(); ++k) fd[k] = split_df_host(h.fval[k]);
       c.fdf.upload(fd.data(), fd.size(), c.st, &c.h2d);
@@ -691,20 +677,11 @@ static void launch_fwd(Ctx& c, const T* fv, const T* X, int64_t xstride, const d
 // MODE 3 R = F.X - P.
 template <int MODE>
 static void fwd_df(Ctx& c, const double* X, double* R) {
-  const int N = (int)c.h.N, D = (int)c.h.D;
   const int64_t MN = c.h.M * c.h.N;
   require(c.xdf.p, "xdf");
   k_split_df<<<elem_grid(MN), 256, 0, c.st>>>(X, MN, 1.0, c.xdf.p);
   post_launch(c);
-  const DfShape sh = df_shape(N, c.df_rows, c.df_kc);
-  const dim3 grid(cdiv(D, sh.RB), sh.chunks);
-  const int threads = cdiv((int64_t)sh.RB * sh.NC, 32) * 32;
-  const size_t smem = df_smem(sh.RB, sh.NC, sh.KC);
-  if (sh.KC == 64)
-    k_fwd_df<MODE, 64><<<grid, threads, smem, c.st>>>(bands_of(c), c.fdf.p, c.xdf.p, c.P.p, R, sh.RB, sh.NC);
-  else
-    k_fwd_df<MODE, 32><<<grid, threads, smem, c.st>>>(bands_of(c), c.fdf.p, c.xdf.p, c.P.p, R, sh.RB, sh.NC);
-  post_launch(c);
+  launch_fwd_df<MODE>(c, R);
 }
 
 static void objective_stack(Ctx& c, const double* Xs, int B) {
@@ -859,17 +836,15 @@ static void op_dL(Ctx& c) {
     const int D = (int)c.h.D;
     k_split_df<<<elem_grid((int64_t)D * N), 256, 0, c.st>>>(c.R.p, (int64_t)D * N, 1.0, c.rdf.p);
     post_launch(c);
-    const DfShape sh = df_shape(N, c.df_rows, c.df_kc);
-    const dim3 grid(cdiv(M, sh.RB), sh.chunks);
-    const int threads = cdiv((int64_t)sh.RB * sh.NC, 32) * 32;
-    const size_t smem = df_smem(sh.RB, sh.NC, sh.KC);
     double* g = c.fullspace ? c.G.p : nullptr;
-    if (sh.KC == 64)
-      k_trans_df<64><<<grid, threads, smem, c.st>>>(bands_of(c), c.tdf.p, c.rdf.p, c.X.p, 2.0 * c.h.gam, sh.RB, sh.NC,
-                                                    g, c.Gf.p);
-    else
-      k_trans_df<32><<<grid, threads, smem, c.st>>>(bands_of(c), c.tdf.p, c.rdf.p, c.X.p, 2.0 * c.h.gam, sh.RB, sh.NC,
-                                                    g, c.Gf.p);
+    const double c2g = 2.0 * c.h.gam;
+    const int rb = df_rows_per_block(M, N, c.df_rows, c.num_sms);
+    const dim3 grid(cdiv(M, rb), cdiv(N, 32 * kDfColWarps));
+    const int threads = 32 * std::min(kDfColWarps, cdiv(N, 32));
+    DevBands bd = bands_of(c);
+    if (rb == 8) k_trans_df<8><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
+    else if (rb == 4) k_trans_df<4><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
+    else k_trans_df<2><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
     post_launch(c);
     if (!c.fullspace) {
       k_reduced_from_full<<<M, std::min(256, std::max(32, cdiv(N, 32) * 32)), 0, c.st>>>(c.Gf.p, c.maxr.p, N, c.G.p);
@@ -1112,7 +1087,7 @@ static void tc_forward(Ctx& c, int splits1, int persistent, const double* pred) 
 // (2 F.V)^T split (written by the first product's epilogue), then the
 // partials of F^T.(2 F.V) in hpart32 (tc_splits of them).
 static void tc_hvp_products(Ctx& c, const float* src, const double* pred, bool presplit) {
-  const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
+  const int M = (int)c.h.M, N = (int)c.h.N;
   if (!presplit) {
     k_split_t<<<dim3(cdiv(M, 32), cdiv(N, 32)), dim3(32, 8), 0, c.st>>>(src, M, N, c.tc_mp, c.vt_hi.p, c.vt_lo.p,
                                                                          pred);
@@ -2713,11 +2688,9 @@ int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "df_products must be -1, 0 or 1");
       c->df_option = (int)value;
     } else if (n == "df_rows") {
-      if (value < 0 || value > 32) throw pqdts::Err(PQDTS_E_ARG, "df_rows must be 0..32");
+      if (value != 0 && value != 2 && value != 4 && value != 8)
+        throw pqdts::Err(PQDTS_E_ARG, "df_rows must be 0, 2, 4 or 8");
       c->df_rows = (int)value;
-    } else if (n == "df_kc") {
-      if (value != 0 && value != 32 && value != 64) throw pqdts::Err(PQDTS_E_ARG, "df_kc must be 0, 32 or 64");
-      c->df_kc = (int)value;
     } else {
       throw pqdts::Err(PQDTS_E_ARG, "unknown option " + n);
     }
@@ -2750,7 +2723,6 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     else if (n == "tensor_cores") *value = c->tc_option;
     else if (n == "df_products") *value = c->df_option;
     else if (n == "df_rows") *value = c->df_rows;
-    else if (n == "df_kc") *value = c->df_kc;
     else if (n == "sched.df_fwd") *value = c->df_fwd;
     else if (n == "sched.df_trans") *value = c->df_trans;
     else if (n == "graphs.captured") *value = (int64_t)c->graphs.size();
