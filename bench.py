@@ -10,9 +10,10 @@ One "step" = one full solve.
   FP64 (the drop-in, `value`): the reference's stopping rule conv < 1e-6.
     The trajectory is bitwise the CPU restatement's, so the CPU baseline does
     exactly the same iterations and reaches exactly the same objective L64.
-  mixed (reported beside it): FP32 Hessian products / CG with FP64 gradient,
-    objective, line search and projection, run until its objective is within
-    1e-8 relative of L64 (an extra stopping rule, off by default).
+  mixed (reported beside it): tensor-core (split-BF16x3) Hessian products /
+    FP32 CG, gradient and objective checks in double-FP32 (~2^-46 relative),
+    FP64 line-search decisions and projection, run until its objective is
+    within 1e-8 relative of L64 (an extra stopping rule, off by default).
 `value` = seconds per solve with the problem resident in HBM (CUDA events on
 the library's stream); `e2e` = the same through the C ABI with host buffers
 (problem upload, starting point upload, solve, result download inside the
@@ -586,7 +587,10 @@ def run_workload(name, args):
                 st = s.solve(mode=2, maxiter=iters, eps=EPS)
                 el = time.perf_counter() - t0
                 bf = s.timer("BF")
+                tl, tg = s.timer("L"), s.timer("dL")
                 out[tag] = {"seconds": el, "outer": st["outer"], "cg": st["cg"],
+                            "L_seconds": tl[0], "L_calls": tl[1], "dL_seconds": tg[0], "dL_calls": tg[1],
+                            "double_fp32": bool(s.get_option("sched.df_fwd")) if prec == pq.MIXED else False,
                             "s_per_outer": el / max(1, st["outer"]), "L": st["L"],
                             "tensor_cores": bool(s.get_option("sched.tc")) if prec == pq.MIXED else False,
                             "bf_seconds": bf[0], "bf_calls": bf[1],
