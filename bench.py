@@ -11,7 +11,7 @@ One "step" = one full solve.
     The trajectory is bitwise the CPU restatement's, so the CPU baseline does
     exactly the same iterations and reaches exactly the same objective L64.
   mixed (reported beside it): tensor-core (split-BF16x3) Hessian products /
-    FP32 CG, gradient and objective checks in double-FP32 (~2^-46 relative),
+    FP32 CG, gradient and objective checks in double-FP32 (~1e-13 relative),
     FP64 line-search decisions and projection, run until its objective is
     within 1e-8 relative of L64 (an extra stopping rule, off by default).
 `value` = seconds per solve with the problem resident in HBM (CUDA events on

@@ -70,8 +70,9 @@ int pqdts_cuda_kernel_launches(pqdts_ctx* ctx, int64_t* count);
  *              1..8: K segments of the tensor-core F.V product.
  *   "df_products" -1 (default, auto) / 1: the mixed path's gradient F^T.R
  *              and its objective checks (residual F.X - P) in double-FP32
- *              (pairs of FP32 numbers, ~2^-46 relative to the sum of the
- *              terms' magnitudes) on the CUDA cores; 0: native FP64.  Takes
+ *              (pairs of FP32 numbers, ~sqrt(K) * 2^-48 relative to the
+ *              sum of the K terms' magnitudes) on the CUDA cores; 0: native
+ *              FP64.  Takes
  *              effect at the next set_problem.  "df_rows" 0 (default,
  *              chosen by size) / 2 / 4 / 8: band rows per block of those
  *              products (each thread accumulates that many outputs).

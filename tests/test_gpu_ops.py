@@ -216,7 +216,7 @@ def _df_instances():
 @pytest.mark.parametrize("full", [True, False])
 def test_L_dL_double_float(built, request, which, full):
     """The mixed path's objective and gradient products in double-FP32
-    (pairs of FP32 numbers): ~2^-46 relative to the terms' magnitudes, so L
+    (pairs of FP32 numbers): ~sqrt(K) * 2^-48 relative to the terms' magnitudes, so L
     within 1e-12 relative and dL within 1e-11 of max|dL| of the FP64 oracle."""
     import pqdts_gb300 as pq
     from oracle.oracle import Oracle
