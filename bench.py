@@ -391,9 +391,9 @@ def run_ours(args):
                 sm.set_option("tensor_cores", tc)
                 sm.set_instance(inst, pq.MIXED)
                 timed_solves(sm, args.warmup, 1e-300, target)
-                b0 = sm.timer("BF")
+                b0, l0, g0 = sm.timer("BF"), sm.timer("L"), sm.timer("dL")
                 mt, ms = timed_solves(sm, args.steps, 1e-300, target)
-                b1 = sm.timer("BF")
+                b1, l1, g1 = sm.timer("BF"), sm.timer("L"), sm.timer("dL")
                 mval = statistics.mean(mt)
                 cgs = sum(x["cg"] for x in ms)
                 bft = b1[0] - b0[0]
@@ -402,6 +402,11 @@ def run_ours(args):
                        "rel_obj_vs_L64": (ms[-1]["L"] - L64) / L64, "reached": ms[-1]["L"] <= target,
                        "outer": ms[-1]["outer"], "cg": ms[-1]["cg"], "refine": ms[-1]["refine"],
                        "tensor_cores": bool(sm.get_option("sched.tc")),
+                       "double_fp32_gradient_and_checks": bool(sm.get_option("sched.df_trans")),
+                       # GPU time per solve in the objective (L: checks of the chosen
+                       # steps) and gradient (dL) regions, double-FP32 products included
+                       "L_region_s_per_solve": (l1[0] - l0[0]) / len(mt),
+                       "dL_region_s_per_solve": (g1[0] - g0[0]) / len(mt),
                        "max_abs_pi_vs_fp64": float(np.max(np.abs(sm.get_x() - X64))),
                        "hessian_product_pair": {"us_per_cg_iteration": bft / cgs * 1e6 if cgs else None,
                                                 "algorithmic_tflops": flops_pair * cgs / bft / 1e12 if bft else None}}

@@ -98,8 +98,9 @@ int pqdts_cuda_set_verbose(pqdts_ctx* ctx, int32_t verbose);
  * Frows, pqdts.f90:77-83, 1357-1363): row d covers columns
  * band_lo[d]..band_hi[d] (band_lo[d] = -1: empty row) and its values are
  * consecutive in band_vals.  P_ND is (D, N) row-major.  precision:
- * PQDTS_FP64 or PQDTS_MIXED (FP32 Hessian products and CG vectors, FP64
- * gradient, objective, line search, projections). */
+ * PQDTS_FP64 or PQDTS_MIXED (FP32 / tensor-core Hessian products and CG
+ * vectors; gradient and objective products in double-FP32, option
+ * "df_products"; FP64 line-search decisions and projections). */
 int pqdts_cuda_set_problem(pqdts_ctx* ctx, int64_t M, int64_t N, int64_t D, const int64_t* band_lo,
                            const int64_t* band_hi, const double* band_vals, const double* P_ND, double gamma,
                            int32_t precision);
@@ -135,7 +136,9 @@ int pqdts_cuda_get_maxr(pqdts_ctx* ctx, int32_t* maxr);
 
 /* Per-operation entry points on the context's X (parity and benchmarking).
  * Like the reference, L, dL and conv_test rebuild X's max column first in
- * the reduced space, and conv_test switches to the full space.  */
+ * the reduced space, and conv_test switches to the full space.  On a
+ * PQDTS_MIXED problem L, dL and conv_test use the mixed solver's products
+ * (double-FP32 unless "df_products" is 0); redO, BF and Bdiag are FP64. */
 int pqdts_cuda_L(pqdts_ctx* ctx, double* val);                     /* L, pqdts.f90:917-973 */
 int pqdts_cuda_dL(pqdts_ctx* ctx, double* G_colmajor);             /* dL, pqdts.f90:975-1032 */
 int pqdts_cuda_redO(pqdts_ctx* ctx, double* O_ND);                 /* redO local part, 707-736 */
