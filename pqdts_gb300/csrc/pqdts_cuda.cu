@@ -1566,9 +1566,10 @@ static void line_search(Ctx& c, bool stage2, double& alpha, double& dlalpha) {
 //   L(X_a) - L(X0) = sum F.dX (2 r0 + F.dX) + Lgam(X_a) - Lgam(X0),
 // dX = X_a - X0 (projected), products in FP32 and sums in FP64 (the change
 // itself to ~1e-6 relative, where a difference of FP32 objectives would be
-// off by ~1e-2); the chosen step then gets an FP64 objective and
-// sufficient-decrease check, and if it fails the reference's FP64 sequence
-// continues from the next probe.
+// off by ~1e-2); the chosen step then gets an objective to FP64 accuracy
+// (double-FP32 product unless that option is off, FP64 sums) and the
+// sufficient-decrease check, and if it fails the reference's sequence
+// continues from the next probe with such objectives.
 static void line_search_mixed(Ctx& c, bool stage2, double& alpha, double& dlalpha) {
   Scope s(c.timers, "Lalpha_min");
   const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
@@ -1771,8 +1772,8 @@ static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
     if (c.precision == PQDTS_MIXED && !c.refine && !c.fullspace && (st.alpha == 0.0 || st.dlalpha >= 0.0))
       c.refine = true;
   }
-  // Mixed path: the chosen step was evaluated in FP64 as a line-search
-  // candidate (projected, rebuilt, its residual and objective known): adopt
+  // Mixed path: the chosen step was evaluated to FP64 accuracy as a
+  // line-search candidate (projected, rebuilt, its residual and objective known): adopt
   // it instead of recomputing the same projection and banded product.
   int adopt = -1;
   if (!c.exact && st.alpha != 0.0 && c.cand_xver == c.xver && c.cand_stage2 == !c.fullspace)
