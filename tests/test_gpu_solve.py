@@ -212,3 +212,57 @@ def test_tiny_shapes(built, shape):
         Xm = s.get_x()
     assert np.isfinite(sm["L"])
     _feasible(Xm)
+
+
+def _gapped(inst):
+    """The instance with one middle row of F emptied: the columns its band
+    covered are then supported on a non-contiguous range of d."""
+    import dataclasses
+
+    d0 = inst.D // 2
+    off = inst.band_offsets()
+    w = np.where(inst.band_lo >= 0, inst.band_hi - inst.band_lo + 1, 0)
+    assert w[d0] > 0
+    keep = np.ones(inst.nnz, bool)
+    keep[off[d0]:off[d0] + w[d0]] = False
+    lo, hi = inst.band_lo.copy(), inst.band_hi.copy()
+    lo[d0], hi[d0] = -1, -2
+    return dataclasses.replace(inst, band_lo=lo, band_hi=hi, band_val=inst.band_val[keep])
+
+
+def test_noncontiguous_columns(built, small):
+    """F with an empty middle row: the transposed products that need
+    contiguous columns are not used (FP64: the CSR form, the oracle's
+    trajectory bit for bit; mixed: the double-FP32 forward product with the
+    native FP64 transposed one)."""
+    import pqdts_gb300 as pq
+    from oracle.oracle import Oracle
+
+    inst = _gapped(small)
+    o = Oracle.from_instance(inst)
+    with pq.Solver(0) as s:
+        s.set_instance(inst)
+        assert s.get_option("sched.trans_rows") == 0
+        st = s.solve(mode=2, maxiter=200, eps=inst.eps)
+        X = s.get_x()
+    Xo, so = o.solve(mode=2, maxiter=200, eps=inst.eps)
+    assert st["L"] == so["L"] and st["cg"] == so["cg"] and np.array_equal(X, Xo)
+    rng = np.random.default_rng(4)
+    Xr = rng.random((inst.M, inst.N))
+    Xr = np.asfortranarray(Xr / Xr.sum(axis=1, keepdims=True))
+    with pq.Solver(0) as s:
+        s.set_instance(inst, pq.MIXED)
+        assert s.get_option("sched.df_fwd") == 1 and s.get_option("sched.df_trans") == 0
+        s.set_space(True, None)
+        s.set_x(Xr)
+        Lg = s.L()
+        G = s.dL()
+        sm = s.solve(mode=2, maxiter=200, eps=inst.eps)
+        Xm = s.get_x()
+    o.set_space(True, None)
+    Lo, _ = o.L(Xr)
+    Go, _ = o.dL(Xr)
+    assert abs(Lg - Lo) <= 1e-12 * abs(Lo)
+    assert np.max(np.abs(G - Go)) <= 1e-11 * np.max(np.abs(Go))
+    assert np.isfinite(sm["L"])
+    _feasible(Xm)
