@@ -175,6 +175,14 @@ int pqdts_cuda_simplexproj(pqdts_ctx* ctx, const double* y, double* x, int64_t l
 enum { PQDTS_NOALLOC_SCRATCH = 1 << 20 };
 int pqdts_cuda_simplexproj_noalloc(const double* d_y, double* d_x, int64_t len, int64_t rows, void* stream);
 
+/* Smoothing of a restart state (pqdts.f90:1877-1902, used when smo_fact > 0
+ * with a starting point read from file): each row j > 100 (1-based) of X
+ * (M, N column-major, host memory, in place) becomes the mean of rows
+ * max(1, j-d)..min(M, j+d), d = nint(j / smo_fact), summed in ascending
+ * order, then is divided by its sum; rows 1..100 are kept.  Needs no device
+ * or context. */
+int pqdts_cuda_smooth(int64_t M, int64_t N, double smo_fact, double* X_colmajor);
+
 /* Solve statistics filled by the solve entry points (may be null):
  * [0] final L  [1] final conv  [2] ||der||  [3] outer iterations
  * [4] CG iterations  [5] line-search L evaluations  [6] FP64 refinement

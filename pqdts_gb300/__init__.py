@@ -78,6 +78,7 @@ def lib():
         "pqdts_cuda_set_option": [p, C.c_char_p, i64],
         "pqdts_cuda_get_option": [p, C.c_char_p, C.POINTER(i64)],
         "pqdts_cuda_solve_batch": [i32, i32, p, p, p, p, p, p, p, p, p, p, p, i32, i32, i32, d, p, p, p],
+        "pqdts_cuda_smooth": [i64, i64, d, p],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -337,3 +338,59 @@ def solve_batch(instances, X0=None, precision=FP64, mode=2, maxiter=100, eps=1e-
         out.append(X[off : off + m * n].reshape((m, n), order="F"))
         off += m * n
     return out, [dict(zip(STAT_KEYS, stats[8 * j : 8 * j + 8].tolist())) for j in range(k)]
+
+
+def smooth(X, smo_fact):
+    """Smoothing of a restart state (pqdts.f90:1877-1902, pqdts_cuda_smooth,
+    host only): a copy of X (M x N) whose rows j > 100 are the mean of the
+    rows within nint(j / smo_fact) of j, renormalised to sum 1."""
+    Xs = np.array(X, dtype=np.float64, order="F", copy=True)
+    if Xs.ndim != 2:
+        raise ValueError("X must be M x N")
+    rc = lib().pqdts_cuda_smooth(Xs.shape[0], Xs.shape[1], float(smo_fact), _ptr(Xs))
+    if rc != 0:
+        raise PqdtsError(f"pqdts_cuda_smooth failed ({rc})")
+    return Xs
+
+
+def run_pqdts(N, M, D, P, threads=1, pqdtspath=None, maxiter=100, tol=1e-6, gamma=0, smo_int=0, smo_dist=0,
+              start_stage=1, smo_fact=0, output=1, verbose=False, F=None, initial=None, dry=False, benchops=0,
+              precision=FP64, device=0):
+    """In-process counterpart of the reference wrapper's run_pqdts
+    (pqdts.py:30-109): the same arguments with the same meaning and the same
+    result, the POVM X (M x N) of the mode-2 solve, without the wrapper's
+    data files (COO triplets and a dense copy of F, pqdts.py:15-28, 36-57)
+    and without a subprocess.
+
+    P (D x N) and F (D x M; None: the internal F, needs M == (D-1)^2) are
+    scipy sparse matrices or arrays, passed on as the COO triplets the
+    wrapper would write; `initial` (M x N) is the starting point, smoothed
+    first when smo_fact > 0 (the wrapper's read_input = 1 path).  threads,
+    pqdtspath (OpenMP threads, the executable) and smo_int, smo_dist
+    (unused by the reference too) are accepted and ignored; dry returns None
+    without solving, as the wrapper's dry run returns before executing;
+    output >= 1 makes no files here (the result is returned); benchops is
+    the executable's operation benchmark (pqdts_cuda.x ... bench = 1) and
+    raises here.  precision / device choose the GPU path."""
+    import scipy.sparse as sps
+
+    if benchops:
+        raise ValueError("benchops: run the executable (pqdts_cuda.x, last argument 1)")
+    Pc = sps.coo_array(P)
+    Fc = None if F is None else sps.coo_array(F)
+    if Pc.shape != (D, N) or (Fc is not None and Fc.shape != (D, M)):
+        raise ValueError("P must be D x N and F D x M")
+    X0 = None
+    if initial is not None:
+        X0 = np.asarray(initial, dtype=np.float64).reshape((M, N))
+        if smo_fact > 0:
+            X0 = smooth(X0, smo_fact)
+    if dry:
+        return None
+    with Solver(device, verbose) as s:
+        s.set_problem_coo(M, N, D, None if Fc is None else (Fc.row, Fc.col, Fc.data), (Pc.row, Pc.col, Pc.data),
+                          gamma, precision)
+        if X0 is not None:
+            s.set_x(X0)
+        s.solve(mode=2, maxiter=maxiter, eps=tol, start_stage=start_stage, output=output)
+        return s.get_x()

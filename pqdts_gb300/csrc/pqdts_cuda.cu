@@ -2594,6 +2594,41 @@ int pqdts_cuda_simplexproj(pqdts_ctx* c, const double* y, double* x, int64_t len
   });
 }
 
+int pqdts_cuda_smooth(int64_t M, int64_t N, double smo_fact, double* X) {
+  if (M <= 0 || N <= 0 || !X || !(smo_fact > 0)) return PQDTS_E_ARG;
+  try {
+    // rows are independent: split them over host threads (same values)
+    std::vector<double> Y(X, X + (size_t)M * N);
+    auto rows = [&](int64_t j0, int64_t j1) {
+      for (int64_t j = std::max<int64_t>(j0, 101); j < j1; ++j) {
+        const int64_t dist = (int64_t)std::llround((double)j / smo_fact);
+        const int64_t k0 = std::max<int64_t>(1, j - dist), k1 = std::min(j + dist, M);
+        double rs = 0;
+        for (int64_t i = 0; i < N; ++i) {
+          double s = 0;
+          int64_t c = 0;
+          for (int64_t k = k0; k <= k1; ++k) {
+            s = s + X[(k - 1) + i * M];
+            c++;
+          }
+          Y[(j - 1) + i * M] = s / (double)c;
+        }
+        for (int64_t i = 0; i < N; ++i) rs += Y[(j - 1) + i * M];
+        for (int64_t i = 0; i < N; ++i) Y[(j - 1) + i * M] = Y[(j - 1) + i * M] / rs;
+      }
+    };
+    const int64_t nt = std::max<int64_t>(1, std::min<int64_t>(std::thread::hardware_concurrency(), (M + 255) / 256));
+    std::vector<std::thread> pool;
+    for (int64_t t = 0; t < nt; ++t) pool.emplace_back(rows, 1 + M * t / nt, 1 + M * (t + 1) / nt);
+    for (auto& th : pool) th.join();
+    std::copy(Y.begin(), Y.end(), X);
+  } catch (const std::exception& e) {
+    fprintf(stderr, "pqdts_cuda_smooth: %s\n", e.what());
+    return PQDTS_E_STATE;
+  }
+  return PQDTS_OK;
+}
+
 int pqdts_cuda_simplexproj_noalloc(const double* d_y, double* d_x, int64_t len, int64_t rows, void* stream) {
   if (!d_y || !d_x || len <= 0 || rows <= 0) {
     fprintf(stderr, "pqdts_cuda_simplexproj_noalloc: null buffer or non-positive size\n");

@@ -263,25 +263,7 @@ int main(int argc, char** argv) {
       memcpy(X.data(), rec.data(), X.size() * 8);
       fclose(f);
       t.stop("input");
-      if (smo_fact > 0) {
-        std::vector<double> Y(X);
-        for (int64_t j = 101; j <= M; ++j) {
-          const int64_t dist = (int64_t)std::llround((double)j / smo_fact);
-          for (int64_t i = 0; i < N; ++i) {
-            double s = 0;
-            int64_t c = 0;
-            for (int64_t k = std::max<int64_t>(1, j - dist); k <= std::min(j + dist, M); ++k) {
-              s = s + X[(k - 1) + i * M];
-              c++;
-            }
-            Y[(j - 1) + i * M] = s / (double)c;
-          }
-          double rs = 0;
-          for (int64_t i = 0; i < N; ++i) rs += Y[(j - 1) + i * M];
-          for (int64_t i = 0; i < N; ++i) Y[(j - 1) + i * M] = Y[(j - 1) + i * M] / rs;
-        }
-        X.swap(Y);
-      }
+      if (smo_fact > 0 && pqdts_cuda_smooth(M, N, smo_fact, X.data()) != PQDTS_OK) return fail(ctx, "smooth");
       if (pqdts_cuda_set_x(ctx, X.data()) != PQDTS_OK) return fail(ctx, "set_x");
     }
   }

@@ -259,5 +259,13 @@ module pqdts_cuda_mod
       real(c_double), value :: conv_thres
       type(c_ptr), value :: target_L
     end function
+
+    ! smoothing of a restart state, pqdts.f90:1877-1902 (host memory, no context)
+    integer(c_int32_t) function pqdts_cuda_smooth(M, N, smo_fact, X) bind(C, name="pqdts_cuda_smooth")
+      import :: c_int32_t, c_int64_t, c_double
+      integer(c_int64_t), value :: M, N
+      real(c_double), value :: smo_fact
+      real(c_double) :: X(*)
+    end function
   end interface
 end module pqdts_cuda_mod

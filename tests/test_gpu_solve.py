@@ -266,3 +266,37 @@ def test_noncontiguous_columns(built, small):
     assert np.max(np.abs(G - Go)) <= 1e-11 * np.max(np.abs(Go))
     assert np.isfinite(sm["L"])
     _feasible(Xm)
+
+
+def test_run_pqdts_in_process(built):
+    """pqdts_gb300.run_pqdts (the wrapper's run_pqdts without data files or a
+    subprocess) gives the oracle's solution bit for bit: F from a sparse
+    matrix, a smoothed starting point, and the internal F."""
+    import scipy.sparse as sps
+
+    import pqdts_gb300 as pq
+    from oracle.oracle import Oracle
+    from pqdts_gb300 import synth
+
+    inst = synth.make_instance(M=150, N=10, D=300, xmax=110.0, eta=0.85, shots=10**5, gamma=1e-3, eps=1e-6, seed=8)
+    r, c, v = inst.coo_F()
+    F = sps.coo_array((v, (r, c)), shape=(inst.D, inst.M))
+    P = sps.csr_array(inst.P)
+    o = Oracle.from_instance(inst)
+    X = pq.run_pqdts(inst.N, inst.M, inst.D, P, maxiter=100, tol=inst.eps, gamma=inst.gamma, F=F)
+    Xo, _ = o.solve(mode=2, maxiter=100, eps=inst.eps)
+    assert np.array_equal(X, Xo)
+    rng = np.random.default_rng(3)
+    X0 = rng.random((inst.M, inst.N))
+    X0 /= X0.sum(axis=1, keepdims=True)
+    X = pq.run_pqdts(inst.N, inst.M, inst.D, P, maxiter=100, tol=inst.eps, gamma=inst.gamma, F=F, initial=X0,
+                     smo_fact=20.0)
+    Xo, _ = o.solve(pq.smooth(X0, 20.0), mode=2, maxiter=100, eps=inst.eps)
+    assert np.array_equal(X, Xo)
+    M, N, D = 64, 6, 9  # internal F: M == (D-1)^2
+    Pd = rng.random((D, N))
+    Pd /= Pd.sum(axis=1, keepdims=True)
+    X = pq.run_pqdts(N, M, D, sps.csr_array(Pd), maxiter=50, tol=1e-6, gamma=1e-4)
+    Pc = sps.coo_array(Pd)
+    Xo, _ = Oracle(M, N, D, 1e-4, None, (Pc.row, Pc.col, Pc.data)).solve(mode=2, maxiter=50, eps=1e-6)
+    assert np.array_equal(X, Xo)
