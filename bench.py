@@ -8,8 +8,9 @@ bit-identical on every platform), solved from Pi = 1/N.
 
 One "step" = one full solve.
   FP64 (the drop-in, `value`): the reference's stopping rule conv < 1e-6.
-    The trajectory is bitwise the CPU restatement's, so the CPU baseline does
-    exactly the same iterations and reaches exactly the same objective L64.
+    The trajectory is bitwise the CPU restatement's (checked in the same run:
+    `config.parity`), so the CPU baseline does exactly the same iterations
+    and reaches exactly the same objective L64.
   mixed (reported beside it): tensor-core (split-BF16x3) Hessian products /
     FP32 CG, gradient and objective checks in double-FP32 (~1e-13 relative),
     FP64 line-search decisions and projection, run until its objective is
@@ -17,12 +18,19 @@ One "step" = one full solve.
 `value` = seconds per solve with the problem resident in HBM (CUDA events on
 the library's stream); `e2e` = the same through the C ABI with host buffers
 (problem upload, starting point upload, solve, result download inside the
-timed region).
+timed region).  With one GPU the line also carries the metric's mixed /
+batched comparisons as full time-to-solution: `config3` (M=10^4, N=10^3,
+D=2*10^4) and `batch` (64 uneven instances), each with its clock record.
+
+Several GPUs: one process per GPU, every rank solves the same instance
+(replicas, no collective in the data path), the step time is the max over
+ranks and the ranks' iteration counts are checked identical.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
   python bench.py --impl reference ...   # the CPU restatement on host cores
 """
 import argparse
+import hashlib
 import json
 import math
 import os
@@ -40,10 +48,9 @@ CONFIG = 2
 EPS = 1e-6          # the reference's convergence threshold for this workload
 OBJ_REL = 1e-8      # mixed precision: objective within 1e-8 relative of L64
 MAXITER = 2000
-# Full-solve work of the default workload (FP64 trajectory, identical for the
-# GPU path and the CPU restatement): outer iterations, CG iterations,
-# line-search objective evaluations.  Used to scale the CPU samples.
-FULL_SOLVE_WORK = (75, 1010, 417)  # measured: FP64 solve of seed 0, bitwise the restatement's
+# identical in both arms' lines (the same instance and stopping rule)
+WORKLOAD = ("M=2000 N=200 D=4000 x_max=1800 eta=0.9 shots=1e7 gamma=1e-5 seed=0, mode-2 two-stage solve from "
+            "Pi=1/N to the reference's stopping rule conv<1e-6 (FP64)")
 
 
 def _passes(outer, cg, ls):
@@ -75,6 +82,7 @@ class Clocks:
                  "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+        return self
 
     def stop(self):
         if not self.proc:
@@ -101,11 +109,19 @@ class Clocks:
 
 
 # --------------------------------------------------------------------------
-# CPU restatement (oracle) sample, run in a clean subprocess so OpenMP sees
+# CPU restatement (oracle) runs, each in a clean subprocess so OpenMP sees
 # the binding environment of pqdts.py (OMP_PROC_BIND, OMP_PLACES).
 # --------------------------------------------------------------------------
-def cpu_sample(config, seed, maxiter, eps, threads):
+def _oracle_subprocess(code, threads):
     env = dict(os.environ, OMP_NUM_THREADS=str(threads), OMP_PROC_BIND="true", OMP_PLACES="cores")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env)
+    if r.returncode != 0:
+        raise RuntimeError("oracle run failed: " + r.stderr[-2000:])
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def cpu_sample(config, seed, maxiter, eps, threads):
+    """The first `maxiter` outer iterations of each stage (a bounded sample)."""
     code = (
         "import json,sys; sys.path.insert(0,%r)\n"
         "from pqdts_gb300 import synth\n"
@@ -115,10 +131,25 @@ def cpu_sample(config, seed, maxiter, eps, threads):
         "o=Oracle.from_instance(inst)\n"
         "X,st=o.solve(mode=2,maxiter=%d,eps=%r)\n"
         "print(json.dumps(st))\n" % (ROOT, threads, config, seed, maxiter, eps))
-    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env)
-    if r.returncode != 0:
-        raise RuntimeError("oracle sample failed: " + r.stderr[-2000:])
-    return json.loads(r.stdout.strip().splitlines()[-1])
+    return _oracle_subprocess(code, threads)
+
+
+def cpu_full_solve(config, seed, eps, threads):
+    """One full solve of the workload: the reference's `min` timer
+    (pqdts.f90:1922, 2168) as `seconds`, the final objective's bits, the
+    iteration counts and a SHA-256 of the final Pi (column-major bytes)."""
+    code = (
+        "import hashlib,json,sys; sys.path.insert(0,%r)\n"
+        "from pqdts_gb300 import synth\n"
+        "from oracle.oracle import Oracle, set_threads\n"
+        "set_threads(%d)\n"
+        "inst=synth.make_config(%d, seed=%d)\n"
+        "o=Oracle.from_instance(inst)\n"
+        "X,st=o.solve(mode=2,maxiter=%d,eps=%r)\n"
+        "st['L_hex']=float(st['L']).hex()\n"
+        "st['pi_sha256']=hashlib.sha256(X.tobytes(order='F')).hexdigest()\n"
+        "print(json.dumps(st))\n" % (ROOT, threads, config, seed, MAXITER, eps))
+    return _oracle_subprocess(code, threads)
 
 
 def host_cores():
@@ -128,21 +159,8 @@ def host_cores():
         return os.cpu_count() or 1
 
 
-def cpu_baseline_value(st_full, config, seed, eps, sample_iters):
-    cores = host_cores()
-    st = cpu_sample(config, seed, sample_iters, eps, cores)
-    work_s = _passes(st["outer"], st["cg"], st["ls"])
-    work_f = _passes(st_full["outer"], st_full["cg"], st_full["ls_evals"])
-    value = st["seconds"] * work_f / work_s
-    return {"value": value, "unit": "s", "cores": cores, "kind": "port",
-            "sample": (f"oracle (C++/OpenMP restatement) on the first {sample_iters} outer iterations of each stage "
-                       f"({int(st['outer'])} outer, {int(st['cg'])} CG, {int(st['ls'])} line-search evaluations, "
-                       f"{st['seconds']:.2f} s), scaled by banded-product passes to the full solve "
-                       f"({work_f:.0f} / {work_s:.0f} passes)")}
-
-
 # --------------------------------------------------------------------------
-# distributed helpers (one process per GPU; independent instances per rank)
+# distributed helpers (one process per GPU; replicas of one instance)
 # --------------------------------------------------------------------------
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -176,42 +194,78 @@ def dist_barrier(dist):
         dist.barrier()
 
 
+def rank_workload(config=CONFIG):
+    """The instance every rank solves: the same seed on every rank (replicas,
+    so the max-over-ranks time measures the same work as one GPU does)."""
+    from pqdts_gb300 import synth
+
+    return synth.make_config(config, seed=0)
+
+
+def replica_check(dist, stats, device):
+    """Per-rank (outer, CG, line-search evaluations, objective) of the last
+    solve, gathered on every rank; `identical` when all ranks did the same
+    work (they solve the same instance, bit for bit)."""
+    row = [float(stats["outer"]), float(stats["cg"]), float(stats.get("ls_evals", stats.get("ls", 0.0))),
+           float(stats["L"])]
+    if dist is None:
+        rows = [row]
+    else:
+        import torch
+
+        t = torch.tensor(row, dtype=torch.float64, device=device)
+        out = [torch.zeros_like(t) for _ in range(dist.get_world_size())]
+        dist.all_gather(out, t)
+        rows = [x.cpu().tolist() for x in out]
+    return replica_summary(rows)
+
+
+def replica_summary(rows):
+    """rows[r] = (outer, CG, line-search evaluations, objective) of rank r."""
+    return {"identical": all(list(r) == list(rows[0]) for r in rows),
+            "per_rank": [{"outer": r[0], "cg": r[1], "ls_evals": r[2], "L": r[3]} for r in rows]}
+
+
 # --------------------------------------------------------------------------
 # reference arm: the CPU restatement on the host cores
 # --------------------------------------------------------------------------
 def run_reference(args):
+    """`value` = one full solve of the workload, timed (the `min` timer);
+    each step = a bounded sample of the same solve (the first k outer
+    iterations of each stage), so K + W steps end within minutes; the
+    samples' seconds per banded-product pass times the full solve's passes
+    is reported beside it as a cross-check."""
     world, rank, _ = dist_env()
     if rank != 0:
         return 0
     cores = host_cores()
     samples = []
-    info = None
     for k in range(args.warmup + args.steps):
         st = cpu_sample(CONFIG, 0, args.ref_sample_iters, EPS, cores)
         if k >= args.warmup:
             samples.append(st)
-        info = st
-    if FULL_SOLVE_WORK is None:
-        work_f = None
-    else:
-        work_f = _passes(*FULL_SOLVE_WORK)
-    per_pass = [s["seconds"] / _passes(s["outer"], s["cg"], s["ls"]) for s in samples]
-    sec_per_pass = statistics.mean(per_pass)
-    value = sec_per_pass * work_f if work_f else None
-    unit = "s" if work_f else "s per banded-product pass"
-    if value is None:
-        value = sec_per_pass
+    t0 = time.perf_counter()
+    full = cpu_full_solve(CONFIG, 0, EPS, cores)
+    full_wall = time.perf_counter() - t0
+    value = full["seconds"]
+    per_pass = statistics.mean(s["seconds"] / _passes(s["outer"], s["cg"], s["ls"]) for s in samples)
+    est = per_pass * _passes(full["outer"], full["cg"], full["ls"])
+    unit = "s"
     line = {
         "impl": "reference", "metric": "time-to-solution at 1e-8 rel. objective (mode-2 solve, s)", "value": value,
         "unit": unit, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": statistics.mean(s["seconds"] for s in samples) * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, pqdts_gb300.synth)",
-        "config": {"workload": "M=2000 N=200 D=4000 mode-2 two-stage solve to conv<1e-6 (FP64)", "threads": cores},
+        "config": {"workload": WORKLOAD, "threads": cores},
+        "step": (f"one bounded sample of the same solve: the first {args.ref_sample_iters} outer iterations of each "
+                 f"stage; `value` is the full solve below"),
+        "full_solve": {"seconds": value, "wall_s": full_wall, "outer": full["outer"], "cg": full["cg"],
+                       "L": full["L"], "L_hex": full["L_hex"], "pi_sha256": full["pi_sha256"]},
+        "pass_scaled_estimate_s": est,
         "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "kind": "port",
-                         "sample": f"oracle restatement, first {args.ref_sample_iters} outer iterations per stage, "
-                                   f"scaled by banded-product passes to the full solve"},
+                         "sample": "one full solve of the workload by the oracle (C++/OpenMP restatement of "
+                                   "pqdts.f90), all host cores, OMP_PROC_BIND=true OMP_PLACES=cores"},
         "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "last_sample": info,
     }
     print(json.dumps(line))
     return 0
@@ -262,35 +316,125 @@ def profile_traffic(name):
     return None
 
 
+def pi_sha256(X):
+    return hashlib.sha256(X.tobytes(order="F")).hexdigest()
+
+
+def timed_solve(solver, device, eps, target=0.0, maxiter=MAXITER):
+    """One solve from Pi = 1/N timed with CUDA events on the library's stream."""
+    import torch
+
+    stream = torch.cuda.ExternalStream(solver.stream(), device=device)
+    solver.set_objective_target(target)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    solver.init_x()
+    st = solver.solve(mode=2, maxiter=maxiter, eps=eps)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) * 1e-3, st
+
+
+def north_star_config3(local, dev):
+    """Full time-to-solution at M=10^4, N=10^3, D=2*10^4: the FP64 GPU solve to
+    conv < 1e-6, then the mixed solver (tensor-core and CUDA-core Hessian
+    products) to an objective within 1e-8 relative of the FP64 one; the error
+    of the mixed Pi and objective against the FP64 result."""
+    import numpy as np
+
+    import pqdts_gb300 as pq
+    from pqdts_gb300 import synth
+
+    t0 = time.perf_counter()
+    inst = synth.make_config(3, seed=0)
+    out = {"workload": "M=10000 N=1000 D=20000 x_max=9000 eta=0.75 shots=1e8 gamma=1e-6 seed=0, mode-2 solve "
+                       "from Pi=1/N", "nnz_F": inst.nnz, "generation_s": time.perf_counter() - t0}
+    clk = Clocks(local).start()
+    with pq.Solver(local) as s:
+        s.set_instance(inst, pq.FP64)
+        timed_solve(s, dev, EPS, maxiter=2)  # warm-up: captures both stages' CG graphs
+        t64, st64 = timed_solve(s, dev, EPS)
+        X64 = s.get_x()
+    L64 = st64["L"]
+    out["fp64"] = {"seconds": t64, "stop": "conv < 1e-6", "L": L64, "outer": st64["outer"], "cg": st64["cg"]}
+    for tc, key in ((-1, "mixed"), (0, "mixed_cuda_cores")):
+        with pq.Solver(local) as s:
+            s.set_option("tensor_cores", tc)
+            s.set_instance(inst, pq.MIXED)
+            timed_solve(s, dev, 1e-300, L64 * (1.0 + OBJ_REL))  # warm-up
+            tm, sm = timed_solve(s, dev, 1e-300, L64 * (1.0 + OBJ_REL))
+            Xm = s.get_x()
+            out[key] = {"seconds": tm, "speedup_vs_fp64": t64 / tm, "stop": "objective <= L64*(1+1e-8)",
+                        "L": sm["L"], "rel_obj_vs_fp64": (sm["L"] - L64) / L64, "reached": sm["L"] <= L64 * (1 + OBJ_REL),
+                        "max_abs_pi_vs_fp64": float(np.max(np.abs(Xm - X64))), "min_pi": float(Xm.min()),
+                        "max_row_sum_err": float(np.max(np.abs(Xm.sum(axis=1) - 1.0))),
+                        "outer": sm["outer"], "cg": sm["cg"], "refine": sm["refine"],
+                        "tensor_cores": bool(s.get_option("sched.tc"))}
+    out["clocks"] = clk.stop()
+    return out
+
+
+def north_star_batch(local, maxiter):
+    """64 uneven instances (8 base detectors x 8 resampled P, gamma swept
+    1e-7..1e-2) through pqdts_cuda_solve_batch, host buffers in and out:
+    FP64 at conv < 1e-6, then mixed precision to within 1e-8 relative of each
+    FP64 objective.  Wall time of each batched call."""
+    import numpy as np
+
+    import pqdts_gb300 as pq
+    from pqdts_gb300 import synth
+
+    t0 = time.perf_counter()
+    insts = synth.make_batch(seed=0)
+    out = {"workload": "batch of %d instances: M log-uniform 500..5000, N 50..500, D=2M, 8 base detectors x 8 "
+                       "resampled P (1e7 shots), gamma 1e-7..1e-2, seed=0" % len(insts),
+           "generation_s": time.perf_counter() - t0, "nnz_F_total": int(sum(i.nnz for i in insts))}
+    clk = Clocks(local).start()
+    t0 = time.perf_counter()
+    X64, st64 = pq.solve_batch(insts, precision=pq.FP64, maxiter=maxiter, eps=EPS, device=local)
+    t64 = time.perf_counter() - t0
+    L64 = np.array([x["L"] for x in st64])
+    t0 = time.perf_counter()
+    Xm, stm = pq.solve_batch(insts, precision=pq.MIXED, maxiter=maxiter, eps=1e-300, targets=L64 * (1.0 + OBJ_REL),
+                             device=local)
+    tmix = time.perf_counter() - t0
+    out["clocks"] = clk.stop()
+    Lm = np.array([x["L"] for x in stm])
+    rel = (Lm - L64) / np.abs(L64)
+    out["fp64"] = {"seconds": t64, "stop": "conv < 1e-6 per instance", "outer_total": sum(x["outer"] for x in st64),
+                   "cg_total": sum(x["cg"] for x in st64)}
+    out["mixed"] = {"seconds": tmix, "speedup_vs_fp64": t64 / tmix, "stop": "objective <= L64*(1+1e-8) per instance",
+                    "outer_total": sum(x["outer"] for x in stm), "cg_total": sum(x["cg"] for x in stm),
+                    "max_rel_objective_vs_fp64": float(rel.max()),
+                    "instances_at_target": int((Lm <= L64 * (1.0 + OBJ_REL)).sum()), "instances": len(insts),
+                    "min_pi": float(min(x.min() for x in Xm)),
+                    "max_abs_pi_vs_fp64": float(max(np.max(np.abs(a - b)) for a, b in zip(Xm, X64)))}
+    out["mixed"]["reached"] = out["mixed"]["instances_at_target"] == len(insts)
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
 
     import pqdts_gb300 as pq
-    from pqdts_gb300 import synth
 
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     dist = dist_init(world, True)
     prec = pq.MIXED if args.precision == "mixed" else pq.FP64
-    inst = synth.make_config(CONFIG, seed=rank)
+    inst = rank_workload()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
 
     def timed_solves(solver, nsteps, eps, target=0.0):
-        stream = torch.cuda.ExternalStream(solver.stream(), device=dev)
-        solver.set_objective_target(target)
         ts, sts = [], []
         for _ in range(nsteps):
             flush.fill_(1.0)  # L2 flush between steps (torch's stream, outside the events)
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            solver.init_x()
-            sts.append(solver.solve(mode=2, maxiter=MAXITER, eps=eps))
-            e1.record(stream)
-            e1.synchronize()
-            ts.append(e0.elapsed_time(e1) * 1e-3)
+            t, st = timed_solve(solver, dev, eps, target)
+            ts.append(t)
+            sts.append(st)
         return ts, sts
 
     # FP64 reference solution of this instance (the drop-in's result): L64
@@ -298,6 +442,7 @@ def run_ours(args):
     s64.set_instance(inst, pq.FP64)
     _, st64 = timed_solves(s64, 1, EPS)
     L64 = st64[0]["L"]
+    X64 = s64.get_x()
     target = L64 * (1.0 + OBJ_REL)
 
     if prec == pq.FP64:
@@ -327,6 +472,8 @@ def run_ours(args):
         assert all(x["L"] == L64 for x in stats), "FP64 solve is not deterministic"
     else:
         assert stats[-1]["L"] <= target, f"mixed solve ended at {stats[-1]['L']} above the target {target}"
+    replicas = replica_check(dist, stats[-1], dev)
+    assert replicas["identical"], f"ranks did different work on the same instance: {replicas}"
 
     # roofline of the dominant kernels: the banded products of the CG's
     # Hessian product (k_fwd + k_trans), FP64- (or FP32-) ALU bound.
@@ -374,7 +521,7 @@ def run_ours(args):
             se.set_instance(inst, prec)
             se.set_x(X0)
             se.solve(mode=2, maxiter=MAXITER, eps=eps_run)
-            Xe = se.get_x()
+            se.get_x()
             e2e_times.append(time.perf_counter() - t0)
             a1 = se.transfer_bytes()
             h2d, d2h = a1[0] - a0[0], a1[1] - a0[1]
@@ -384,19 +531,20 @@ def run_ours(args):
     # time to an objective within 1e-8 relative of L64
     extra = {}
     if prec == pq.FP64 and args.with_mixed and world == 1:
-        X64 = s64.get_x()  # the FP64 solve's result (the last timed solve)
-
         def mixed_run(tc):
             with pq.Solver(local) as sm:
                 sm.set_option("tensor_cores", tc)
                 sm.set_instance(inst, pq.MIXED)
                 timed_solves(sm, args.warmup, 1e-300, target)
                 b0, l0, g0 = sm.timer("BF"), sm.timer("L"), sm.timer("dL")
+                ck = Clocks(local).start()
                 mt, ms = timed_solves(sm, args.steps, 1e-300, target)
+                mclk = ck.stop()
                 b1, l1, g1 = sm.timer("BF"), sm.timer("L"), sm.timer("dL")
                 mval = statistics.mean(mt)
                 cgs = sum(x["cg"] for x in ms)
                 bft = b1[0] - b0[0]
+                Xm = sm.get_x()
                 out = {"value": mval, "unit": "s", "speedup_vs_fp64": step_s / mval,
                        "stop": "objective <= L64*(1+1e-8)", "objective": ms[-1]["L"],
                        "rel_obj_vs_L64": (ms[-1]["L"] - L64) / L64, "reached": ms[-1]["L"] <= target,
@@ -407,20 +555,43 @@ def run_ours(args):
                        # steps) and gradient (dL) regions, double-FP32 products included
                        "L_region_s_per_solve": (l1[0] - l0[0]) / len(mt),
                        "dL_region_s_per_solve": (g1[0] - g0[0]) / len(mt),
-                       "max_abs_pi_vs_fp64": float(np.max(np.abs(sm.get_x() - X64))),
+                       "max_abs_pi_vs_fp64": float(np.max(np.abs(Xm - X64))), "min_pi": float(Xm.min()),
+                       "max_row_sum_err": float(np.max(np.abs(Xm.sum(axis=1) - 1.0))),
                        "hessian_product_pair": {"us_per_cg_iteration": bft / cgs * 1e6 if cgs else None,
-                                                "algorithmic_tflops": flops_pair * cgs / bft / 1e12 if bft else None}}
+                                                "algorithmic_tflops": flops_pair * cgs / bft / 1e12 if bft else None},
+                       "clocks": mclk}
                 return out
         extra["mixed"] = mixed_run(-1)
         if extra["mixed"]["tensor_cores"]:
             extra["mixed"]["cuda_core_variant"] = mixed_run(0)
 
+    # parity and CPU baseline in one: the oracle's full solve of the same
+    # instance on the host cores, compared with the FP64 GPU result bit for bit
     cpu = None
+    parity = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
-            cpu = cpu_baseline_value(st64[0], CONFIG, rank, EPS, args.cpu_sample_iters)
+            cores = host_cores()
+            full = cpu_full_solve(CONFIG, 0, EPS, cores)
+            cpu = {"value": full["seconds"], "unit": "s", "cores": cores, "kind": "port",
+                   "sample": "one full solve of the same instance by the oracle (C++/OpenMP restatement of "
+                             "pqdts.f90), all host cores, OMP_PROC_BIND=true OMP_PLACES=cores; the reference's "
+                             "`min` timer"}
+            gpu = {"L_hex": float(L64).hex(), "outer": st64[0]["outer"], "cg": st64[0]["cg"],
+                   "pi_sha256": pi_sha256(X64)}
+            parity = {"against": "oracle full solve, same instance",
+                      "objective_bitwise": gpu["L_hex"] == full["L_hex"],
+                      "counts_equal": gpu["outer"] == full["outer"] and gpu["cg"] == full["cg"],
+                      "pi_bitwise": gpu["pi_sha256"] == full["pi_sha256"],
+                      "gpu": gpu, "oracle": {k: full[k] for k in ("L_hex", "outer", "cg", "pi_sha256")}}
+            parity["bitwise"] = parity["objective_bitwise"] and parity["counts_equal"] and parity["pi_bitwise"]
         except Exception as e:  # reported, never silently replaced
             cpu = {"value": None, "error": str(e)[:300]}
+
+    # the metric's mixed / batched comparisons at full time-to-solution
+    if prec == pq.FP64 and world == 1 and args.north_star:
+        extra["config3"] = north_star_config3(local, dev)
+        extra["batch"] = north_star_batch(local, args.batch_maxiter)
 
     if rank == 0:
         line = {
@@ -428,14 +599,14 @@ def run_ours(args):
             "value": step_s, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": step_s * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if prec == pq.FP64 else "f32+f64",
-            "data": "synthetic (seeded, pqdts_gb300.synth; rank r uses seed r)",
-            "config": {"workload": "M=2000 N=200 D=4000 x_max=1800 eta=0.9 shots=1e7 gamma=1e-5, "
-                                   "mode-2 two-stage solve from Pi=1/N (FP64: to conv<1e-6; mixed: to 1e-8 rel. "
-                                   "of the FP64 objective)",
+            "data": "synthetic (seeded, pqdts_gb300.synth; every rank solves the seed-0 instance)",
+            "config": {"workload": WORKLOAD,
                        "nnz_F": nnz, "precision": args.precision, "l2": "flushed between steps (256 MiB write)",
                        "objective": stats[-1]["L"], "objective_fp64": L64,
                        "rel_obj_vs_fp64": rel_err, "outer": stats[-1]["outer"], "cg": stats[-1]["cg"],
-                       "ls_evals": stats[-1]["ls_evals"], "parallelism": f"{world} independent instance(s)"},
+                       "ls_evals": stats[-1]["ls_evals"], "parallelism": f"{world} replica(s) of one instance",
+                       "parity": parity},
+            "replicas": replicas,
             "solves_per_s": world / step_s,
             "wall_s_timed_region": t_wall,
             "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -616,7 +787,6 @@ def main():
     ap.add_argument("--with-mixed", dest="with_mixed", action="store_true", default=True)
     ap.add_argument("--no-mixed", dest="with_mixed", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample-iters", type=int, default=4)
     ap.add_argument("--ref-sample-iters", type=int, default=3)
     ap.add_argument("--profile-case", choices=["fp64", "mixed", "solve64", "solvemix", "tc3", "tcdense", "tc3p",
                                                "tcdensep"], default=None,
@@ -624,6 +794,8 @@ def main():
     ap.add_argument("--workload", choices=["batch", "config3", "dense", "config5"], default=None,
                     help="secondary measurement instead of the bench line")
     ap.add_argument("--batch-maxiter", type=int, default=200)
+    ap.add_argument("--no-north-star", dest="north_star", action="store_false", default=True,
+                    help="skip the config3 / batch time-to-solution keys of the bench line")
     ap.add_argument("--batch-sequential", action="store_true",
                     help="batch workload: also time the FP64 solves one after another")
     ap.add_argument("--config3-iters", type=int, default=3)

@@ -76,6 +76,18 @@ int pqdts_cuda_kernel_launches(pqdts_ctx* ctx, int64_t* count);
  *              effect at the next set_problem.  "df_rows" 0 (default,
  *              chosen by size) / 2 / 4 / 8: band rows per block of those
  *              products (each thread accumulates that many outputs).
+ *   "fp64_refine" 0 (default) / 1: when a mixed-precision solve runs its CG
+ *              in FP64 (the final refinement, counted in stats[6]): 0 from
+ *              the first stage-2 iteration whose FP32 Newton step gives no
+ *              decrease; 1 for every stage-2 iteration.
+ *   "tc_wait_ms" 2000 (default) / 1..60000: limit of each barrier wait in
+ *              the tensor-core kernels; a wait that runs out makes the call
+ *              fail with PQDTS_E_CUDA ("a barrier wait timed out"), the
+ *              kernel having stored nothing and freed its tensor memory, and
+ *              the context stays usable.
+ *   "tc_wait_probe" 0 (default) / 1: test hook of that error path -- the
+ *              kernels' copy producer first waits on a barrier that nothing
+ *              arrives on, so the wait runs out before any copy or MMA.
  * Unknown names return PQDTS_E_ARG. */
 int pqdts_cuda_set_option(pqdts_ctx* ctx, const char* name, int64_t value);
 /* Reads an option above or a field of the schedule in use:
@@ -157,6 +169,18 @@ int pqdts_cuda_conv_test(pqdts_ctx* ctx, double* conv);            /* conv_test,
  * pqdts.f90:1133). */
 int pqdts_cuda_simplexproj(pqdts_ctx* ctx, const double* y, double* x, int64_t len, int64_t rows);
 
+/* The reference's own symbol, with its exact signature (condat_simplexproj.c:60;
+ * pqdts.f90:1133 calls it as simplexproj_Condat(x3, x2, n2) through an
+ * implicit interface, which gfortran resolves to this name): x[0..len-1]
+ * receives the projection of y onto the unit simplex, bitwise equal to the
+ * reference's.  No context argument and no return value: each host thread
+ * gets its own stream and device buffers on the current device (threads may
+ * call it concurrently on private buffers, as the reference's OpenMP loop
+ * does); x == y is allowed; on a CUDA failure a message goes to stderr and x
+ * is filled with NaN.  Linking pqdts.f90 against libpqdts_cuda.so instead of
+ * condat_simplexproj.c needs no source change. */
+void simplexproj_condat_(double* y, double* x, int* plength);
+
 /* The same projection for callers that cannot allocate device memory, e.g.
  * a host that owns all device memory through its own pool and forbids other
  * allocations after start-up.  No counterpart in the reference.  Needs no
@@ -167,7 +191,9 @@ int pqdts_cuda_simplexproj(pqdts_ctx* ctx, const double* y, double* x, int64_t l
  * that capacity is rejected with PQDTS_E_ARG and a message on stderr.
  * Runs asynchronously on `stream` (a cudaStream_t; NULL = legacy default
  * stream) of the current device.  The first call on a device looks up the
- * scratch address on that device; make that first call before any stream
+ * scratch address on that device, and so does the first call after that
+ * device's current CUDA context has changed (a cudaDeviceReset, or a
+ * caller's own driver-API context); make that first call before any stream
  * capture.  All calls share the one scratch array (its contents are fully
  * rewritten before use, nothing needs clearing), so calls whose kernels can
  * overlap on the GPU -- different streams, different host threads -- race

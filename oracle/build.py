@@ -19,7 +19,10 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_TREE = os.environ.get("PQDTS_REFERENCE_TREE", "/root/reference")
+# The reference tree: PQDTS_REFERENCE_TREE, else a checkout named
+# `reference` beside this repository; absent (the GPU machine) -> skipped.
+REFERENCE_TREE = os.environ.get("PQDTS_REFERENCE_TREE") or os.path.join(os.path.dirname(os.path.dirname(HERE)),
+                                                                         "reference")
 
 
 def _flags():

@@ -11,10 +11,10 @@
 // machine, so pqdts_omp.x cannot be run.  What IS pinned:
 //   * the simplex projection (condat_project below) is bit-exact against the
 //     reference's own condat_simplexproj.c, compiled from the reference tree
-//     into oracle/_ref by oracle/build.py (tests/test_oracle_condat.py);
+//     into oracle/_ref by oracle/build.py (tests/test_oracle.py);
 //   * the derivative identities of the reference's built-in self test
 //     (pqdts.f90:1737-1831) hold for L/dL/BF/Bdiag in full and reduced space
-//     (tests/test_oracle_derivatives.py).
+//     (tests/test_oracle.py).
 //
 // Arithmetic conventions (what makes this restatement deterministic):
 //   * Reductions follow one fixed order of the reference: every Fortran

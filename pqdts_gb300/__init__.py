@@ -382,7 +382,9 @@ def run_pqdts(N, M, D, P, threads=1, pqdtspath=None, maxiter=100, tol=1e-6, gamm
         raise ValueError("P must be D x N and F D x M")
     X0 = None
     if initial is not None:
-        X0 = np.asarray(initial, dtype=np.float64).reshape((M, N))
+        # Fortran order as the wrapper writes it (pqdts.py:57): a flat
+        # length-M*N input is X column by column, a 2-D one is X itself
+        X0 = np.asarray(initial, dtype=np.float64).reshape((M, N), order="F")
         if smo_fact > 0:
             X0 = smooth(X0, smo_fact)
     if dry:

@@ -351,6 +351,7 @@ struct pqdts_ctx {
   pqdts::GpuTimers timers;
   int64_t n_cg = 0, n_lsL = 0, n_refine = 0;
   bool refine = false;  // mixed precision: FP64 CG from now on
+  int refine_option = 0;  // 1: mixed precision runs the FP64 CG for all of stage 2
   double target_L = 0.0;  // optional objective stopping rule (0 = off)
   // version of X, bumped on every write; results keyed on it are reused
   int64_t xver = 0, R_ver = -1, G_ver = -1, L_ver = -1, rebuilt_ver = -1;
@@ -373,6 +374,8 @@ struct pqdts_ctx {
   int tc_option = -1;
   int tc_persistent_option = -1;  // -1 autotuned, 0 one CTA per tile, 1 persistent
   int tc_splits1_option = -1;     // -1 autotuned, else the K segments of the tensor-core F.V product
+  uint64_t tc_wait_ns = pqdts::kTcWaitNs;  // limit of each mbarrier wait in the tensor-core kernels
+  int tc_wait_probe = 0;                   // 1: their producer waits on a barrier nothing arrives on (test hook)
   int rows_option = -1;           // row-flattened FP64 products: -1 autotuned, 0 never, 1 always (where they apply)
   int num_sms = 0;
   bool tc_ready = false;
@@ -396,11 +399,44 @@ using Ctx = pqdts_ctx;
 
 // Scratch of pqdts_cuda_simplexproj_noalloc: Condat's per-row working lists.
 // In host code this name is only a stand-in for the symbol; the device
-// address comes from cudaGetSymbolAddress, once per device.
+// address comes from cudaGetSymbolAddress, once per device and CUDA context
+// (the context's unique id is kept with it: a device reset or a caller's own
+// driver-API context on the same device gets its own lookup).
 static __device__ __align__(256) double g_noalloc_scratch[PQDTS_NOALLOC_SCRATCH];
 constexpr int kMaxDevices = 64;
 static std::mutex g_noalloc_mu;
-static double* g_noalloc_ptr[kMaxDevices] = {};
+struct NoallocSlot {
+  double* ptr = nullptr;
+  unsigned long long ctx_id = 0;
+};
+static NoallocSlot g_noalloc[kMaxDevices];
+
+// Unique id of the calling thread's current CUDA context (0: none or the
+// driver entry points are unavailable -- then the address is looked up on
+// every call, which allocates nothing either).
+static unsigned long long current_ctx_id() {
+  typedef CUresult (*GetCurrentFn)(CUcontext*);
+  typedef CUresult (*GetIdFn)(CUcontext, unsigned long long*);
+  static std::once_flag once;
+  static GetCurrentFn get_current = nullptr;
+  static GetIdFn get_id = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (GetCurrentFn)p;
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (GetIdFn)p;
+  });
+  if (!get_current || !get_id) return 0;
+  CUcontext cur = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&cur) != CUDA_SUCCESS || cur == nullptr || get_id(cur, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 static DevBands bands_of(Ctx& c) {
   DevBands b;
@@ -437,6 +473,17 @@ static void reduce_to(Ctx& c, const double* part, int64_t count, double* out, in
 static void read_back(Ctx& c, const double* dev, int count) {
   CK(cudaMemcpyAsync(c.pin, dev, count * sizeof(double), cudaMemcpyDeviceToHost, c.st));
   CK(cudaStreamSynchronize(c.st));
+}
+
+// After a read-back of the scalars: a tensor-core kernel whose bounded
+// barrier wait ran out has set SC_TCERR.  The flag is cleared (the kernels
+// freed their tensor memory and stored nothing, the context stays usable)
+// and the call fails with PQDTS_E_CUDA.
+static void check_tc_error(Ctx& c) {
+  if (c.pin[SC_TCERR] == 0.0) return;
+  CK(cudaMemsetAsync(c.sc.p + SC_TCERR, 0, sizeof(double), c.st));
+  CK(cudaStreamSynchronize(c.st));
+  throw Err(PQDTS_E_CUDA, "tensor-core product: a barrier wait timed out");
 }
 
 // ---------------------------------------------------------------------------
@@ -1056,12 +1103,12 @@ static void tc_product(Ctx& c, const TcOperand& A, const CUtensorMap& bhi, const
     const int grid = (int)std::min<int64_t>(tiles, c.num_sms);
     k_tc_band_p<<<grid, kTcpThreads, smem, c.st>>>(A.map_hi, A.map_lo, bhi, blo, A.kb.p, A.nch.p, R, N, c.tc_bn,
                                                    c.tc_stages, splits, A.blocks, mode, scale, out, (int64_t)R * N, oh,
-                                                   ol, ld, pred, c.sc.p + SC_TCERR);
+                                                   ol, ld, pred, c.sc.p + SC_TCERR, c.tc_wait_ns, c.tc_wait_probe);
   } else {
     const dim3 grid(cdiv(N, c.tc_bn), A.blocks, splits);
     k_tc_band<<<grid, kTcThreads, smem, c.st>>>(A.map_hi, A.map_lo, bhi, blo, A.kb.p, A.nch.p, R, N, c.tc_bn,
                                                 c.tc_stages, splits, mode, scale, out, (int64_t)R * N, oh, ol, ld, pred,
-                                                c.sc.p + SC_TCERR);
+                                                c.sc.p + SC_TCERR, c.tc_wait_ns, c.tc_wait_probe);
   }
   post_launch(c);
 }
@@ -1255,7 +1302,7 @@ static int cg_chunks(Ctx& c, std::array<uint64_t, 4> variant, Iter&& iteration) 
       for (int k = 0; k < chunk && queued < kMaxCG; ++k, ++queued) iteration(queued == 0);
       read_back(c, c.sc.p, SC_NSC);
     }
-    if (c.pin[SC_TCERR] != 0.0) throw Err(PQDTS_E_CUDA, "tensor-core product: a barrier wait timed out");
+    check_tc_error(c);
     if (c.pin[SC_DONE] != 0.0 || queued >= kMaxCG) return (int)c.pin[SC_ITER];
   }
 }
@@ -1756,6 +1803,7 @@ static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
     }
     op_dL(c);
     const double bdfac = c.fullspace ? 1.0 : 2.0;
+    if (c.precision == PQDTS_MIXED && c.refine_option == 1 && !c.fullspace) c.refine = true;
     const bool fp32 = (c.precision == PQDTS_MIXED) && !c.refine;
     if (fp32) cg_solve32(c, bdfac);
     else cg_solve<double>(c, c.cg64, c.fval.p, c.tval.p, bdfac, nullptr);
@@ -1903,6 +1951,26 @@ static void fill_stats(Ctx& c, const SolveState& st, double secs, double* stats)
   stats[7] = secs;
 }
 
+// Mixed path, end of a stage: Pi >= 0 exactly.  Rows with a negative entry
+// are projected onto the simplex in place (a change of ~1e-12 at most, the
+// size of the reference's own tolerance, pqdts.f90:424); when any row moved,
+// the reported objective is that of the projected X (conv stays the stage's
+// last conv_test).  The FP64 drop-in keeps the reference's -1e-12 allowance
+// and its bit-exact iterate.
+static void nonneg_x(Ctx& c, SolveState& st) {
+  const int M = (int)c.h.M, N = (int)c.h.N;
+  CK(cudaMemsetAsync(c.icount.p, 0, sizeof(long long), c.st));
+  k_nonneg_rows<<<cdiv((int64_t)M * 32, 256), 256, 0, c.st>>>(c.X.p, M, N, (unsigned long long*)c.icount.p);
+  post_launch(c);
+  long long moved = 0;
+  CK(cudaMemcpyAsync(&moved, c.icount.p, sizeof(long long), cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+  if (moved == 0) return;
+  touch_x(c);
+  c.fullspace = true;
+  st.L0 = op_L(c);
+}
+
 static void solve(Ctx& c, int mode, int maxiiter, double conv_thres, int start_stage, int output, pqdts_stage_cb cb,
                   void* user, double* stats) {
   need_problem(c);
@@ -1932,6 +2000,7 @@ static void solve(Ctx& c, int mode, int maxiiter, double conv_thres, int start_s
   c.target_hit = false;
   for (int oiter = start_stage; oiter <= 2 && !c.target_hit; ++oiter) {
     run_stage(c, mode, oiter, maxiiter, conv_thres, output, st);
+    if (c.precision == PQDTS_MIXED) nonneg_x(c, st);
     if (cb) {
       std::vector<double> xh((size_t)c.h.M * c.h.N);
       get_x_colmajor(c, xh.data());
@@ -2225,7 +2294,7 @@ static void choose_schedule(Ctx& c) {
     c.hpart32.release();
   }
   read_back(c, c.sc.p, SC_NSC);
-  if (c.pin[SC_TCERR] != 0.0) throw Err(PQDTS_E_CUDA, "tensor-core product: a barrier wait timed out");
+  check_tc_error(c);
 }
 
 // Problem set-up shared by the entry points.
@@ -2529,7 +2598,7 @@ int pqdts_cuda_BF32(pqdts_ctx* c, const double* V, double* HV) {
     pqdts::hvp32(*c, b, nullptr, false, nullptr);
     CK(cudaMemcpyAsync(rm.data(), b.Hp.p, rm.size() * 4, cudaMemcpyDeviceToHost, c->st));
     pqdts::read_back(*c, c->sc.p, pqdts::SC_NSC);
-    if (c->pin[pqdts::SC_TCERR] != 0.0) throw Err(PQDTS_E_CUDA, "tensor-core product: a barrier wait timed out");
+    pqdts::check_tc_error(*c);
     c->d2h += (int64_t)rm.size() * 4;
     for (int64_t i = 0; i < M; ++i)
       for (int64_t n = 0; n < N; ++n) HV[i + n * M] = rm[(size_t)i * N + n];
@@ -2594,6 +2663,66 @@ int pqdts_cuda_simplexproj(pqdts_ctx* c, const double* y, double* x, int64_t len
   });
 }
 
+// The reference's own projection symbol (condat_simplexproj.c:60, called
+// from doproj at pqdts.f90:1133 through an implicit interface), so pqdts.f90
+// links against this library unchanged.  Its signature has no context and
+// no error return: each host thread (the reference calls it from OpenMP
+// threads on private buffers) lazily gets its own stream and device buffers
+// on the current device.  x receives the projection of y (x doubles as the
+// reference's scratch; here y is copied to the device first, so x == y also
+// gives the projection).  On a CUDA failure a message goes to stderr and x
+// is filled with NaN, which the caller's objective then shows.
+namespace pqdts {
+struct CondatThreadState {
+  int device = -1;
+  cudaStream_t st = nullptr;
+  double* buf = nullptr;  // 2 * cap doubles: the row, then Condat's working list
+  int64_t cap = 0;
+  void release() noexcept {
+    if (buf) cudaFree(buf);
+    if (st) cudaStreamDestroy(st);
+    buf = nullptr;
+    st = nullptr;
+    cap = 0;
+    device = -1;
+  }
+  ~CondatThreadState() { release(); }
+};
+static thread_local CondatThreadState t_condat;
+}  // namespace pqdts
+
+void simplexproj_condat_(double* y, double* x, int* plength) {
+  if (!y || !x || !plength || *plength <= 0) return;
+  const int len = *plength;
+  pqdts::CondatThreadState& t = pqdts::t_condat;
+  cudaError_t e = cudaSuccess;
+  auto fail = [&](const char* what) {
+    fprintf(stderr, "simplexproj_condat_: %s: %s\n", what, cudaGetErrorString(e));
+    for (int i = 0; i < len; ++i) x[i] = std::numeric_limits<double>::quiet_NaN();
+  };
+  int dev = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return fail("no current device");
+  if (t.device != dev) {
+    t.release();
+    if ((e = cudaStreamCreateWithFlags(&t.st, cudaStreamNonBlocking)) != cudaSuccess) return fail("stream");
+    t.device = dev;
+  }
+  if (t.cap < len) {
+    if (t.buf) cudaFree(t.buf);
+    t.buf = nullptr;
+    t.cap = 0;
+    if ((e = cudaMalloc((void**)&t.buf, (size_t)2 * len * sizeof(double))) != cudaSuccess) return fail("allocation");
+    t.cap = len;
+  }
+  double* d = t.buf;
+  double* w = t.buf + t.cap;
+  if ((e = cudaMemcpyAsync(d, y, (size_t)len * 8, cudaMemcpyHostToDevice, t.st)) != cudaSuccess) return fail("upload");
+  pqdts::k_condat<<<1, 32, 0, t.st>>>(d, nullptr, nullptr, d, w, 0, 1, len);
+  if ((e = cudaGetLastError()) != cudaSuccess) return fail("launch");
+  if ((e = cudaMemcpyAsync(x, d, (size_t)len * 8, cudaMemcpyDeviceToHost, t.st)) != cudaSuccess) return fail("download");
+  if ((e = cudaStreamSynchronize(t.st)) != cudaSuccess) return fail("projection");
+}
+
 int pqdts_cuda_smooth(int64_t M, int64_t N, double smo_fact, double* X) {
   if (M <= 0 || N <= 0 || !X || !(smo_fact > 0)) return PQDTS_E_ARG;
   try {
@@ -2648,18 +2777,23 @@ int pqdts_cuda_simplexproj_noalloc(const double* d_y, double* d_x, int64_t len, 
   }
   double* scratch = nullptr;
   {
-    // set-up once per device, with that device current: the scratch's device address
+    // set-up once per device (and context), with that device current: the
+    // scratch's device address
     std::lock_guard<std::mutex> g(pqdts::g_noalloc_mu);
-    if (pqdts::g_noalloc_ptr[dev] == nullptr) {
+    pqdts::NoallocSlot& slot = pqdts::g_noalloc[dev];
+    const unsigned long long id = pqdts::current_ctx_id();
+    if (slot.ptr == nullptr || id == 0 || slot.ctx_id != id) {
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, pqdts::g_noalloc_scratch);
       if (e != cudaSuccess || p == nullptr) {
         fprintf(stderr, "pqdts_cuda_simplexproj_noalloc: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+        slot.ptr = nullptr;
         return PQDTS_E_CUDA;
       }
-      pqdts::g_noalloc_ptr[dev] = static_cast<double*>(p);
+      slot.ptr = static_cast<double*>(p);
+      slot.ctx_id = pqdts::current_ctx_id();  // the lookup may have made the primary context current
     }
-    scratch = pqdts::g_noalloc_ptr[dev];
+    scratch = slot.ptr;
   }
   pqdts::k_condat<<<dim3(pqdts::cdiv(rows, pqdts::kRowThreads), 1), pqdts::kRowThreads, 0, (cudaStream_t)stream>>>(
       d_y, nullptr, nullptr, d_x, scratch, 0, (int)rows, (int)len);
@@ -2682,6 +2816,7 @@ int pqdts_cuda_run_stage(pqdts_ctx* c, int32_t mode, int32_t oiter, int32_t maxi
     const double t0 = pqdts::wall();
     st.t0 = t0;
     pqdts::run_stage(*c, mode, oiter, maxiiter, conv_thres, output, st);
+    if (c->precision == PQDTS_MIXED) pqdts::nonneg_x(*c, st);
     CK(cudaStreamSynchronize(c->st));
     pqdts::fill_stats(*c, st, pqdts::wall() - t0, stats);
   });
@@ -2723,6 +2858,17 @@ int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
     } else if (n == "df_products") {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "df_products must be -1, 0 or 1");
       c->df_option = (int)value;
+    } else if (n == "fp64_refine") {
+      if (value < 0 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "fp64_refine must be 0 or 1");
+      c->refine_option = (int)value;
+    } else if (n == "tc_wait_ms") {
+      if (value < 1 || value > 60000) throw pqdts::Err(PQDTS_E_ARG, "tc_wait_ms must be 1..60000");
+      c->tc_wait_ns = (uint64_t)value * 1000000ull;
+      c->drop_graphs();  // captured launches carry the old limit
+    } else if (n == "tc_wait_probe") {
+      if (value < 0 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "tc_wait_probe must be 0 or 1");
+      c->tc_wait_probe = (int)value;
+      c->drop_graphs();
     } else if (n == "df_rows") {
       if (value != 0 && value != 2 && value != 4 && value != 8)
         throw pqdts::Err(PQDTS_E_ARG, "df_rows must be 0, 2, 4 or 8");
@@ -2759,6 +2905,9 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     else if (n == "tensor_cores") *value = c->tc_option;
     else if (n == "df_products") *value = c->df_option;
     else if (n == "df_rows") *value = c->df_rows;
+    else if (n == "tc_wait_ms") *value = (int64_t)(c->tc_wait_ns / 1000000ull);
+    else if (n == "tc_wait_probe") *value = c->tc_wait_probe;
+    else if (n == "fp64_refine") *value = c->refine_option;
     else if (n == "sched.df_fwd") *value = c->df_fwd;
     else if (n == "sched.df_trans") *value = c->df_trans;
     else if (n == "graphs.captured") *value = (int64_t)c->graphs.size();

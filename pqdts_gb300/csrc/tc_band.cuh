@@ -17,8 +17,13 @@
 // bf16 in, FP32 accumulator in tensor memory), all four warps then read the
 // accumulator back (tcgen05.ld, one row per thread) and store it.
 //
-// Every mbarrier wait is bounded (kTcWaitNs); a wait that runs out sets
-// *err, skips the remaining work and stores nothing.
+// Every mbarrier wait is bounded (wait_ns, by default kTcWaitNs); a wait
+// that runs out sets *err, skips the remaining work and stores nothing, and
+// the CTA frees its tensor memory only after the copies in flight have
+// landed and the MMAs already issued have completed (the issuer's last
+// tcgen05.commit).  `probe` != 0 is a test hook: the producer first waits on
+// a barrier that nothing arrives on, so the wait runs out before any copy or
+// MMA is issued and the error path runs on an otherwise valid launch.
 #pragma once
 
 #include <cuda.h>
@@ -31,7 +36,7 @@ constexpr int kTcThreads = 128;
 constexpr int kTcRows = 128;           // rows of a band block = MMA M
 constexpr int kTcK = 64;               // K per stage: one 128-byte swizzled row of bf16
 constexpr int kTcMaxStages = 4;
-constexpr uint64_t kTcWaitNs = 2000000000ull;  // 2 s per wait
+constexpr uint64_t kTcWaitNs = 2000000000ull;  // 2 s per wait (default)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -61,12 +66,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Wait for the phase of `parity` to complete; false when kTcWaitNs ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Wait for the phase of `parity` to complete; false when limit_ns ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_ns();
   while (!mbar_try_wait(bar, parity))
-    if (global_ns() - t0 > kTcWaitNs) return false;
+    if (global_ns() - t0 > limit_ns) return false;
   return true;
 }
 
@@ -166,10 +171,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               const int32_t* __restrict__ blk_kb, const int32_t* __restrict__ blk_nch, int R, int N, int BN,
               int stages, int splits, int mode, float scale, float* __restrict__ out, int64_t out_stride,
               __nv_bfloat16* __restrict__ oh, __nv_bfloat16* __restrict__ ol, int64_t ld,
-              const double* __restrict__ pred, double* __restrict__ err) {
+              const double* __restrict__ pred, double* __restrict__ err, uint64_t wait_ns, int probe) {
   if (pred != nullptr && pred[6] != 0.0) return;  // CG already converged
   extern __shared__ uint8_t tc_smem_raw[];
-  __shared__ uint64_t bar_full[kTcMaxStages], bar_empty[kTcMaxStages], bar_acc;
+  __shared__ uint64_t bar_full[kTcMaxStages], bar_empty[kTcMaxStages], bar_acc, bar_probe;
   __shared__ uint32_t s_tmem;
   __shared__ volatile int s_abort;
   __shared__ int s_issued, s_consumed;
@@ -201,6 +206,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       mbar_init(&bar_empty[i], 1);
     }
     mbar_init(&bar_acc, 1);
+    mbar_init(&bar_probe, 1);
     s_abort = 0;
     s_issued = 0;
     s_consumed = 0;
@@ -219,10 +225,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
   if (warp == 0 && lane == 0 && nk > 0) {
     // producer: TMA loads of A hi/lo (block-local K) and B hi/lo (global K)
+    if (probe && !mbar_wait(&bar_probe, 0, wait_ns)) s_abort = 1;  // nothing arrives: runs out
     for (int it = 0; it < nk && !s_abort; ++it) {
       const int st = it % stages;
       const uint32_t ph = (uint32_t)(it / stages) & 1u;
-      if (!mbar_wait(&bar_empty[st], ph ^ 1u)) {
+      if (!mbar_wait(&bar_empty[st], ph ^ 1u, wait_ns)) {
         s_abort = 1;
         break;
       }
@@ -242,7 +249,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     for (int it = 0; it < nk && !s_abort; ++it) {
       const int st = it % stages;
       const uint32_t ph = (uint32_t)(it / stages) & 1u;
-      if (!mbar_wait(&bar_full[st], ph)) {
+      if (!mbar_wait(&bar_full[st], ph, wait_ns)) {
         s_abort = 1;
         break;
       }
@@ -259,14 +266,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
       tc_commit(&bar_empty[st]);  // the stage is free once these MMAs are done
     }
-    tc_commit(&bar_acc);
+    tc_commit(&bar_acc);  // also after an abort: arrives once every issued MMA is done
   }
   __syncwarp();
 
   // epilogue: thread t of warp w owns accumulator row 32w + t
   bool ok = true;
   if (nk > 0) {
-    ok = mbar_wait(&bar_acc, 0);
+    ok = mbar_wait(&bar_acc, 0, wait_ns);
     tc_fence_after();
   }
   if (!ok) s_abort = 1;
@@ -336,7 +343,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     *err = 1.0;
     // let the copies already in flight land before the CTA's memory goes
     for (int it = s_consumed; it < s_issued; ++it)
-      if (!mbar_wait(&bar_full[it % stages], (uint32_t)(it / stages) & 1u)) break;
+      if (!mbar_wait(&bar_full[it % stages], (uint32_t)(it / stages) & 1u, wait_ns)) break;
+    // and the MMAs already issued finish with tensor and shared memory
+    // (the issuer committed bar_acc after its last one, aborted or not)
+    if (nk > 0) mbar_wait(&bar_acc, 0, wait_ns);
   }
   __syncthreads();
   if (warp == 0) {
@@ -364,10 +374,11 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
                 const int32_t* __restrict__ blk_kb, const int32_t* __restrict__ blk_nch, int R, int N, int BN,
                 int stages, int splits, int blocks, int mode, float scale, float* __restrict__ out,
                 int64_t out_stride, __nv_bfloat16* __restrict__ oh, __nv_bfloat16* __restrict__ ol, int64_t ld,
-                const double* __restrict__ pred, double* __restrict__ err) {
+                const double* __restrict__ pred, double* __restrict__ err, uint64_t wait_ns, int probe) {
   if (pred != nullptr && pred[6] != 0.0) return;  // CG already converged
   extern __shared__ uint8_t tc_smem_raw[];
-  __shared__ uint64_t bar_full[kTcMaxStages], bar_empty[kTcMaxStages], bar_tfull[2], bar_tempty[2];
+  __shared__ uint64_t bar_full[kTcMaxStages], bar_empty[kTcMaxStages], bar_tfull[2], bar_tempty[2], bar_fin,
+      bar_probe;
   __shared__ uint32_t s_tmem;
   __shared__ volatile int s_abort;
   __shared__ int s_issued, s_consumed;
@@ -395,6 +406,8 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
       mbar_init(&bar_tfull[i], 1);
       mbar_init(&bar_tempty[i], 128);
     }
+    mbar_init(&bar_fin, 1);
+    mbar_init(&bar_probe, 1);
     s_abort = 0;
     s_issued = 0;
     s_consumed = 0;
@@ -429,13 +442,14 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
   if (warp == 0) {
     if (lane == 0) {
       int it = 0;
+      if (probe && !mbar_wait(&bar_probe, 0, wait_ns)) s_abort = 1;  // nothing arrives: runs out
       for (int t = blockIdx.x; t < T && !s_abort; t += gridDim.x) {
         int nt, blk, c0, c1, kb;
         tile(t, nt, blk, c0, c1, kb);
         for (int ch = c0; ch < c1 && !s_abort; ++ch, ++it) {
           const int st = it % stages;
           const uint32_t ph = (uint32_t)(it / stages) & 1u;
-          if (!mbar_wait(&bar_empty[st], ph ^ 1u)) {
+          if (!mbar_wait(&bar_empty[st], ph ^ 1u, wait_ns)) {
             s_abort = 1;
             break;
           }
@@ -460,7 +474,7 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
         tile(t, nt, blk, c0, c1, kb);
         const int buf = j & 1;
         const uint32_t acc = tmem + (uint32_t)buf * ncols;
-        if (!mbar_wait(&bar_tempty[buf], ((uint32_t)(j >> 1) & 1u) ^ 1u)) {  // accumulator free
+        if (!mbar_wait(&bar_tempty[buf], ((uint32_t)(j >> 1) & 1u) ^ 1u, wait_ns)) {  // accumulator free
           s_abort = 1;
           break;
         }
@@ -468,7 +482,7 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
         for (int ch = c0; ch < c1; ++ch, ++it) {
           const int st = it % stages;
           const uint32_t ph = (uint32_t)(it / stages) & 1u;
-          if (!mbar_wait(&bar_full[st], ph)) {
+          if (!mbar_wait(&bar_full[st], ph, wait_ns)) {
             s_abort = 1;
             break;
           }
@@ -487,6 +501,7 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
         }
         tc_commit(&bar_tfull[buf]);  // (also with no MMAs: the epilogue then stores zeros)
       }
+      tc_commit(&bar_fin);  // arrives once every MMA this CTA issued is done (aborted or not)
     }
   } else {
     // epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. + 31 = tile rows
@@ -496,7 +511,7 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
       int nt, blk, c0, c1, kb;
       tile(t, nt, blk, c0, c1, kb);
       const int nk = c1 - c0, buf = j & 1;
-      const bool ok = mbar_wait(&bar_tfull[buf], (uint32_t)(j >> 1) & 1u);
+      const bool ok = mbar_wait(&bar_tfull[buf], (uint32_t)(j >> 1) & 1u, wait_ns);
       tc_fence_after();
       const bool store = __all_sync(0xffffffffu, ok && !s_abort);
       if (!store) {
@@ -547,8 +562,10 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
   __syncthreads();
   if (s_abort && threadIdx.x == 0) {
     *err = 1.0;
+    // copies in flight land, then the issued MMAs finish (the issuer's last commit)
     for (int it = s_consumed; it < s_issued; ++it)
-      if (!mbar_wait(&bar_full[it % stages], (uint32_t)(it / stages) & 1u)) break;
+      if (!mbar_wait(&bar_full[it % stages], (uint32_t)(it / stages) & 1u, wait_ns)) break;
+    mbar_wait(&bar_fin, 0, wait_ns);
   }
   __syncthreads();
   if (warp == 1) {

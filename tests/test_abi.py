@@ -32,6 +32,17 @@ def test_library_exports_all_declared_symbols(built):
     assert not missing, missing
 
 
+def test_library_exports_the_reference_condat_symbol(built):
+    """simplexproj_condat_ (condat_simplexproj.c:60) with its C prototype in
+    the header, exported under that exact name, so pqdts.f90's call at
+    :1133 links against the library unchanged."""
+    import pqdts_gb300 as pq
+
+    src = open(os.path.join(ROOT, "include", "pqdts_cuda.h")).read()
+    assert re.search(r"^void simplexproj_condat_\(double\* y, double\* x, int\* plength\);", src, flags=re.M)
+    assert hasattr(C.CDLL(pq.LIB_PATH), "simplexproj_condat_")
+
+
 def test_no_device_is_an_error_code(built):
     import torch
 

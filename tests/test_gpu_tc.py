@@ -94,7 +94,7 @@ def test_tc_mixed_solve_reaches_fp64_objective(built, tc_insts, persistent):
     X = s.get_x()
     s.close()
     assert abs(st["L"] - st64["L"]) <= 1e-8 * abs(st64["L"]), (st, st64)
-    assert X.min() >= -1e-12 and np.max(np.abs(X.sum(1) - 1.0)) <= 1e-12
+    assert X.min() >= 0.0 and np.max(np.abs(X.sum(1) - 1.0)) <= 1e-12
 
 
 @pytest.mark.parametrize("persistent", [0, 1])
