@@ -358,19 +358,35 @@ def north_star_config3(local, dev):
         X64 = s.get_x()
     L64 = st64["L"]
     out["fp64"] = {"seconds": t64, "stop": "conv < 1e-6", "L": L64, "outer": st64["outer"], "cg": st64["cg"]}
+    flops_pair = 2 * 2.0 * inst.nnz * inst.N  # useful flops of one Hessian product (F.V, then F^T.(2 F.V))
+    peaks = measured_peaks()
     for tc, key in ((-1, "mixed"), (0, "mixed_cuda_cores")):
         with pq.Solver(local) as s:
             s.set_option("tensor_cores", tc)
             s.set_instance(inst, pq.MIXED)
             timed_solve(s, dev, 1e-300, L64 * (1.0 + OBJ_REL))  # warm-up
+            b0 = s.timer("BF")
             tm, sm = timed_solve(s, dev, 1e-300, L64 * (1.0 + OBJ_REL))
+            b1 = s.timer("BF")
             Xm = s.get_x()
+            bft, bfn = b1[0] - b0[0], b1[1] - b0[1]
+            pair = {"calls": bfn, "us_per_call": bft / bfn * 1e6 if bfn else None,
+                    "useful_tflops": flops_pair * bfn / bft / 1e12 if bft else None,
+                    "note": "the CG's Hessian product (operand split, both products, row epilogue) per CG "
+                            "iteration, GPU events in the solve"}
+            if tc != 0 and bft and peaks.get("bf16_tflops"):
+                # split-BF16x3: three bf16 MMA terms per useful product term (plus the zero fill of each
+                # 128-row block's K window, not counted): a lower bound of the tensor pipe's work
+                pair["issued_bf16_tflops_lower_bound"] = 3 * pair["useful_tflops"]
+                pair["frac_of_bf16_peak_lower_bound"] = 3 * pair["useful_tflops"] / peaks["bf16_tflops"]
+                pair["peak_source"] = "MEASURED_PEAKS.json bf16_tflops (burst, of measured)"
+
             out[key] = {"seconds": tm, "speedup_vs_fp64": t64 / tm, "stop": "objective <= L64*(1+1e-8)",
                         "L": sm["L"], "rel_obj_vs_fp64": (sm["L"] - L64) / L64, "reached": sm["L"] <= L64 * (1 + OBJ_REL),
                         "max_abs_pi_vs_fp64": float(np.max(np.abs(Xm - X64))), "min_pi": float(Xm.min()),
                         "max_row_sum_err": float(np.max(np.abs(Xm.sum(axis=1) - 1.0))),
                         "outer": sm["outer"], "cg": sm["cg"], "refine": sm["refine"],
-                        "tensor_cores": bool(s.get_option("sched.tc"))}
+                        "tensor_cores": bool(s.get_option("sched.tc")), "hessian_product": pair}
     out["clocks"] = clk.stop()
     return out
 

@@ -76,6 +76,12 @@ int pqdts_cuda_kernel_launches(pqdts_ctx* ctx, int64_t* count);
  *              effect at the next set_problem.  "df_rows" 0 (default,
  *              chosen by size) / 2 / 4 / 8: band rows per block of those
  *              products (each thread accumulates that many outputs).
+ *   "internal_f" -1 (default) / 0 / 1: where the internal F of
+ *              pqdts_cuda_set_problem_coo (nnzF < 0) is computed: -1 on the
+ *              device for PQDTS_MIXED problems and on the host for PQDTS_FP64
+ *              (the host's libm lgamma / exp / log, as the reference's, keep
+ *              the FP64 drop-in bitwise); 0 host; 1 device (CUDA's lgamma /
+ *              exp / log: values within ~1e-12 relative of the host's).
  *   "fp64_refine" 0 (default) / 1: when a mixed-precision solve runs its CG
  *              in FP64 (the final refinement, counted in stats[6]): 0 from
  *              the first stage-2 iteration whose FP32 Newton step gives no
@@ -249,15 +255,29 @@ int pqdts_cuda_timer(pqdts_ctx* ctx, const char* name, double* seconds, int64_t*
  * per-instance objective targets as pqdts_cuda_set_objective_target.
  * stats: PQDTS_NSTATS per instance.  Host workers (the host's hardware
  * threads up to 16, or the environment variable PQDTS_BATCH_WORKERS; at
- * most one per instance) each own a
- * context and stream and take instances in order, so instances overlap on
- * the device; each context's CG chunks replay as CUDA graphs and instances
- * of one size bucket share one autotuned launch schedule. */
+ * most one per task) each own a context and stream and take tasks in
+ * order, so tasks overlap on the device; each context's CG chunks replay as
+ * CUDA graphs and instances of one size bucket share one autotuned launch
+ * schedule.  A task is one instance, or (PQDTS_MIXED, mode 2, 32 <= N <=
+ * 1024) a group of up to 16 instances with the same M, N, D and identical F
+ * (bands and values: resampled P, gamma sweeps), solved in lockstep: each
+ * member keeps its own line search and stages, and their FP32 CG runs
+ * jointly -- every CG launch serves all members, the tensor-core products
+ * taking the members' vectors as the columns of one wider product.  The
+ * environment variable PQDTS_BATCH_GROUPS=0 turns the grouping off. */
 int pqdts_cuda_solve_batch(int32_t device, int32_t n_inst, const int64_t* M, const int64_t* N, const int64_t* D,
                            const int64_t* band_lo, const int64_t* band_hi, const double* band_vals,
                            const int64_t* band_row_offset, const int64_t* band_val_offset, const double* P,
                            const int64_t* P_offset, const double* gamma, int32_t precision, int32_t mode,
                            int32_t maxiiter, double conv_thres, const double* target_L, double* X, double* stats);
+
+/* The grouping pqdts_cuda_solve_batch uses for a mixed-precision mode-2
+ * batch (same arguments as there): group_of[k] = the group of instance k
+ * (instances solved in lockstep with a joint CG) or -1 (solved alone).  Host
+ * only, needs no device.  No counterpart in the reference. */
+int pqdts_cuda_batch_groups(int32_t n_inst, const int64_t* M, const int64_t* N, const int64_t* D,
+                            const int64_t* band_lo, const int64_t* band_hi, const double* band_vals,
+                            const int64_t* band_row_offset, const int64_t* band_val_offset, int32_t* group_of);
 
 #ifdef __cplusplus
 }

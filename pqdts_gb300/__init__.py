@@ -79,6 +79,7 @@ def lib():
         "pqdts_cuda_get_option": [p, C.c_char_p, C.POINTER(i64)],
         "pqdts_cuda_solve_batch": [i32, i32, p, p, p, p, p, p, p, p, p, p, p, i32, i32, i32, d, p, p, p],
         "pqdts_cuda_smooth": [i64, i64, d, p],
+        "pqdts_cuda_batch_groups": [i32, p, p, p, p, p, p, p, p, p],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -303,11 +304,7 @@ class Solver:
         return s.value, n.value
 
 
-def solve_batch(instances, X0=None, precision=FP64, mode=2, maxiter=100, eps=1e-6, device=0, targets=None):
-    """Solve independent instances (uneven M, N, D, gamma) on one GPU;
-    `targets`: optional per-instance objective targets (stop once L <= it)."""
-    L = lib()
-    k = len(instances)
+def _batch_arrays(instances):
     M = np.array([i.M for i in instances], np.int64)
     N = np.array([i.N for i in instances], np.int64)
     D = np.array([i.D for i in instances], np.int64)
@@ -316,6 +313,29 @@ def solve_batch(instances, X0=None, precision=FP64, mode=2, maxiter=100, eps=1e-
     vals = np.concatenate([i.band_val for i in instances]).astype(np.float64)
     row_off = np.concatenate([[0], np.cumsum(D)[:-1]]).astype(np.int64)
     val_off = np.concatenate([[0], np.cumsum([i.band_val.size for i in instances])[:-1]]).astype(np.int64)
+    return M, N, D, lo, hi, vals, row_off, val_off
+
+
+def batch_groups(instances):
+    """The lockstep groups solve_batch forms for a mixed-precision batch:
+    group index per instance (-1: solved alone).  Host only."""
+    M, N, D, lo, hi, vals, row_off, val_off = _batch_arrays(instances)
+    out = np.empty(len(instances), np.int32)
+    rc = lib().pqdts_cuda_batch_groups(len(instances), _ptr(M), _ptr(N), _ptr(D), _ptr(lo), _ptr(hi), _ptr(vals),
+                                       _ptr(row_off), _ptr(val_off), _ptr(out))
+    if rc != 0:
+        raise PqdtsError(f"pqdts_cuda_batch_groups failed ({rc})")
+    return out
+
+
+def solve_batch(instances, X0=None, precision=FP64, mode=2, maxiter=100, eps=1e-6, device=0, targets=None):
+    """Solve independent instances (uneven M, N, D, gamma) on one GPU;
+    `targets`: optional per-instance objective targets (stop once L <= it).
+    Mixed-precision instances that share F are solved in lockstep groups
+    with a joint CG (batch_groups shows the grouping)."""
+    L = lib()
+    k = len(instances)
+    M, N, D, lo, hi, vals, row_off, val_off = _batch_arrays(instances)
     P = np.concatenate([i.P.ravel() for i in instances]).astype(np.float64)
     P_off = np.concatenate([[0], np.cumsum(D * N)[:-1]]).astype(np.int64)
     gam = np.array([i.gamma for i in instances], np.float64)

@@ -33,6 +33,7 @@
 #include "kernels.cuh"
 #include "problem_host.h"
 #include "tc_band.cuh"
+#include "batch_cg.cuh"
 
 namespace pqdts {
 
@@ -121,6 +122,7 @@ struct GpuTimers {
   std::vector<cudaEvent_t> pool;
   cudaStream_t st = nullptr;
   bool enabled = true;  // Scope regions recorded (off: no events at all)
+  bool detail = false;  // also the per-kernel spans of a CG iteration ("CG.*")
   int id_of(const char* n) {
     for (size_t i = 0; i < names.size(); ++i)
       if (names[i] == n) return (int)i;
@@ -232,6 +234,9 @@ struct Scope {
   GpuTimers& t;
   int tok;
   Scope(GpuTimers& tt, const char* n) : t(tt), tok(tt.enabled ? tt.begin(n) : kOff) {}
+  // a detail span: recorded only at timer level 2
+  Scope(GpuTimers& tt, const char* n, bool detail)
+      : t(tt), tok(tt.enabled && (!detail || tt.detail) ? tt.begin(n) : kOff) {}
   ~Scope() {
     if (tok != kOff) t.end(tok);
   }
@@ -272,13 +277,22 @@ struct Schedule {
 };
 
 // Band operand of the tensor-core products: 128-row blocks of bf16 hi/lo
-// values, block b covering K columns [kb[b], kb[b] + 64 nch[b]), with the
-// TMA maps of both halves (box 64 K x 128 rows, 128-byte swizzle).
+// values, block b covering K columns [kb[b], kb[b] + kTcK nch[b]), with the
+// TMA maps of both halves (box kTcK x 128 rows, swizzled to the row width).
+// Per-CTA tile lists of the persistent tensor-core kernel for one (N tile
+// width, K splits) pair: CTA b takes tile[off[b] .. off[b+1]).
+struct TcSched {
+  DBuf<int32_t> off, tile;
+  int grid = 0;
+};
+
 struct TcOperand {
   DBuf<__nv_bfloat16> hi, lo;
   DBuf<int32_t> kb, nch;
+  std::vector<int32_t> h_nch;  // K chunks per row block (host copy: the tile costs)
   int blocks = 0, kmax = 0;
   CUtensorMap map_hi, map_lo;
+  std::map<std::pair<int, int>, std::unique_ptr<TcSched>> scheds;  // keyed by (BN, splits)
 };
 
 // CG work vectors of one precision.
@@ -352,6 +366,7 @@ struct pqdts_ctx {
   int64_t n_cg = 0, n_lsL = 0, n_refine = 0;
   bool refine = false;  // mixed precision: FP64 CG from now on
   int refine_option = 0;  // 1: mixed precision runs the FP64 CG for all of stage 2
+  int internal_f_option = -1;  // internal F on the device: -1 for mixed problems, 0 never (host), 1 always
   double target_L = 0.0;  // optional objective stopping rule (0 = off)
   // version of X, bumped on every write; results keyed on it are reused
   int64_t xver = 0, R_ver = -1, G_ver = -1, L_ver = -1, rebuilt_ver = -1;
@@ -386,6 +401,10 @@ struct pqdts_ctx {
   pqdts::DBuf<float> ypart;  // FP32 partials of F.V when its K range is split
   CUtensorMap map_vt_hi, map_vt_lo, map_yt_hi, map_yt_lo;
   pqdts::Schedule sched;
+  bool own_stream = true;  // false: a member of a batched group, on the group's stream
+  // group context of a batched lockstep solve: the members' CG table
+  pqdts::DBuf<pqdts::CGMember> memtab;
+  std::vector<pqdts::CGMember> h_memtab;
   void drop_graphs() noexcept {
     for (auto& kv : graphs) kv.second.destroy();
     graphs.clear();
@@ -592,8 +611,8 @@ static void setup_device(Ctx& c) {
   c.cg64.alloc(MN, M, D * N);
   c.sqd.alloc(M);
   CK(cudaFuncSetAttribute(k_condat_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCondatSmemMax));
-  c.counters.alloc(4);
-  CK(cudaMemsetAsync(c.counters.p, 0, 4 * sizeof(unsigned), c.st));
+  c.counters.alloc(8);
+  CK(cudaMemsetAsync(c.counters.p, 0, 8 * sizeof(unsigned), c.st));
   c.exact = (c.precision == PQDTS_FP64);
   // residual stack of the line-search candidates (both precisions)
   c.Rst.alloc((size_t)kBatchLS * D * N);
@@ -978,7 +997,8 @@ static EncodeTiledFn encode_tiled() {
 }
 
 // 2-D bf16 map: inner x outer elements, rows row_bytes apart, box
-// box_inner x box_outer, 128-byte swizzle, zero fill outside the extents.
+// box_inner x box_outer (box_inner * 2 = the stage row width kTcRowBytes,
+// swizzled to match), zero fill outside the extents.
 static void make_map_bf16(CUtensorMap* m, const void* base, uint64_t inner, uint64_t outer, uint64_t row_bytes,
                           uint32_t box_inner, uint32_t box_outer) {
   const cuuint64_t dims[2] = {inner, outer};
@@ -986,7 +1006,10 @@ static void make_map_bf16(CUtensorMap* m, const void* base, uint64_t inner, uint
   const cuuint32_t box[2] = {box_inner, box_outer};
   const cuuint32_t es[2] = {1, 1};
   const CUresult r = encode_tiled()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box,
-                                    es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                    es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                    kTcRowBytes == 128  ? CU_TENSOR_MAP_SWIZZLE_128B
+                                    : kTcRowBytes == 64 ? CU_TENSOR_MAP_SWIZZLE_64B
+                                                        : CU_TENSOR_MAP_SWIZZLE_32B,
                                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) throw Err(PQDTS_E_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
 }
@@ -1028,6 +1051,8 @@ static void build_tc_operand(Ctx& c, const std::vector<int32_t>& lo, const std::
   op.lo.upload(lv.data(), total, c.st, &c.h2d);
   op.kb.upload(kb.data(), blocks, c.st, &c.h2d);
   op.nch.upload(nch.data(), blocks, c.st, &c.h2d);
+  op.h_nch = nch;
+  op.scheds.clear();
   op.blocks = blocks;
   op.kmax = kmax;
   make_map_bf16(&op.map_hi, op.hi.p, kmax, (uint64_t)blocks * kTcRows, (uint64_t)kmax * 2, kTcK, kTcRows);
@@ -1043,7 +1068,7 @@ static int tc_tile_n(int64_t N, int mult) {
   return (int)std::max<int64_t>(16, std::min<int64_t>(256, bn));
 }
 
-static uint32_t tc_stage_bytes(int bn) { return 2u * kTcRows * 128u + 2u * (uint32_t)bn * 128u; }
+static uint32_t tc_stage_bytes(int bn) { return 2u * kTcRows * kTcRowBytes + 2u * (uint32_t)bn * kTcRowBytes; }
 constexpr uint32_t kTcRing = 200u * 1024u;           // stage ring budget
 constexpr uint32_t kTcMaxSmem = kTcRing + 1024u;      // + alignment slack
 
@@ -1053,6 +1078,11 @@ static void tc_configure(Ctx& c, int bn) {
   const int64_t M = c.h.M, N = c.h.N, D = c.h.D;
   const int stages = std::min<int>(kTcMaxStages, (int)(kTcRing / tc_stage_bytes(bn)));
   if (stages < 2) throw Err(PQDTS_E_STATE, "internal: tensor-core stage ring does not fit");
+  // k_tc_band's FP32 epilogue stages the 128 x BN tile (rows padded to an odd
+  // word count) in the ring
+  const uint32_t staging = 128u * (uint32_t)(bn + ((33 - bn % 32) % 32)) * 4u;
+  if ((uint32_t)stages * tc_stage_bytes(bn) < staging)
+    throw Err(PQDTS_E_STATE, "internal: tensor-core epilogue staging does not fit the stage ring");
   make_map_bf16(&c.map_vt_hi, c.vt_hi.p, M, N, (uint64_t)c.tc_mp * 2, kTcK, bn);
   make_map_bf16(&c.map_vt_lo, c.vt_lo.p, M, N, (uint64_t)c.tc_mp * 2, kTcK, bn);
   make_map_bf16(&c.map_yt_hi, c.yt_hi.p, D, N, (uint64_t)c.tc_dp * 2, kTcK, bn);
@@ -1090,20 +1120,67 @@ static void setup_tc(Ctx& c) {
   c.tc_ready = true;
 }
 
+// Tile lists of the persistent kernel for A's row blocks at N tile width bn
+// and K splits `splits`: tiles (N tile fastest, then row block, then split)
+// sorted by their K chunks, longest first, each given to the CTA with the
+// least work so far (+2 chunks of fixed cost per tile); built once per
+// problem and shape, outside any stream capture.
+static TcSched& tc_sched(Ctx& c, TcOperand& A, int bn, int splits) {
+  auto key = std::make_pair(bn, splits);
+  auto it = A.scheds.find(key);
+  if (it != A.scheds.end()) return *it->second;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(c.st, &cs));
+  if (cs != cudaStreamCaptureStatusNone) throw Err(PQDTS_E_STATE, "internal: tensor-core tile lists built in a capture");
+  const int ntn = cdiv(c.h.N, bn);
+  const int64_t T = (int64_t)ntn * A.blocks * splits;
+  const int grid = (int)std::min<int64_t>(T, c.num_sms);
+  std::vector<std::pair<int, int32_t>> cost((size_t)T);
+  for (int64_t t = 0; t < T; ++t) {
+    const int64_t rest = t / ntn;
+    const int blk = (int)(rest % A.blocks), sp = (int)(rest / A.blocks);
+    const int c1 = A.h_nch[blk], per = (c1 + splits - 1) / splits;
+    const int s0 = std::min(c1, sp * per), s1 = std::min(c1, s0 + per);
+    cost[t] = {s1 - s0 + 2, (int32_t)t};
+  }
+  std::stable_sort(cost.begin(), cost.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+  std::vector<std::vector<int32_t>> lists(grid);
+  std::vector<int64_t> load(grid, 0);
+  for (const auto& ct : cost) {
+    const int g = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    load[g] += ct.first;
+    lists[g].push_back(ct.second);
+  }
+  std::vector<int32_t> off(grid + 1, 0), tiles;
+  tiles.reserve((size_t)T);
+  for (int g = 0; g < grid; ++g) {
+    // each CTA walks its tiles in tile order (N tiles of a row block together)
+    std::sort(lists[g].begin(), lists[g].end());
+    tiles.insert(tiles.end(), lists[g].begin(), lists[g].end());
+    off[g + 1] = (int32_t)tiles.size();
+  }
+  auto sc = std::make_unique<TcSched>();
+  sc->off.upload(off.data(), off.size(), c.st, &c.h2d);
+  sc->tile.upload(tiles.data(), tiles.size(), c.st, &c.h2d);
+  sc->grid = grid;
+  CK(cudaStreamSynchronize(c.st));  // the host vectors go out of scope
+  return *A.scheds.emplace(key, std::move(sc)).first->second;
+}
+
 // Out = scale * A . B^T on the tensor cores (A a TcOperand of R rows; B the
 // K-major split operand behind bhi / blo); mode 0: FP32 partials (splits of
 // the K range, out_stride apart), mode 1: transposed bf16 split into oh / ol.
-static void tc_product(Ctx& c, const TcOperand& A, const CUtensorMap& bhi, const CUtensorMap& blo, int R, int splits,
+static void tc_product(Ctx& c, TcOperand& A, const CUtensorMap& bhi, const CUtensorMap& blo, int R, int splits,
                        int mode, float scale, float* out, __nv_bfloat16* oh, __nv_bfloat16* ol, int64_t ld,
                        const double* pred, int persistent) {
   const int N = (int)c.h.N;
   const size_t smem = (size_t)c.tc_stages * tc_stage_bytes(c.tc_bn) + 1024;
   if (persistent) {
-    const int64_t tiles = (int64_t)cdiv(N, c.tc_bn) * A.blocks * splits;
-    const int grid = (int)std::min<int64_t>(tiles, c.num_sms);
-    k_tc_band_p<<<grid, kTcpThreads, smem, c.st>>>(A.map_hi, A.map_lo, bhi, blo, A.kb.p, A.nch.p, R, N, c.tc_bn,
-                                                   c.tc_stages, splits, A.blocks, mode, scale, out, (int64_t)R * N, oh,
-                                                   ol, ld, pred, c.sc.p + SC_TCERR, c.tc_wait_ns, c.tc_wait_probe);
+    TcSched& ts = tc_sched(c, A, c.tc_bn, splits);
+    k_tc_band_p<<<ts.grid, kTcpThreads, smem, c.st>>>(A.map_hi, A.map_lo, bhi, blo, A.kb.p, A.nch.p, R, N, c.tc_bn,
+                                                      c.tc_stages, splits, A.blocks, mode, scale, out, (int64_t)R * N,
+                                                      oh, ol, ld, pred, c.sc.p + SC_TCERR, c.tc_wait_ns,
+                                                      c.tc_wait_probe, ts.off.p, ts.tile.p);
   } else {
     const dim3 grid(cdiv(N, c.tc_bn), A.blocks, splits);
     k_tc_band<<<grid, kTcThreads, smem, c.st>>>(A.map_hi, A.map_lo, bhi, blo, A.kb.p, A.nch.p, R, N, c.tc_bn,
@@ -1140,7 +1217,11 @@ static void tc_hvp_products(Ctx& c, const float* src, const double* pred, bool p
                                                                          pred);
     post_launch(c);
   }
-  tc_forward(c, c.sched.tc_splits1, c.sched.tc_persistent, pred);
+  {
+    Scope sd(c.timers, "CG.tc_fwd", true);
+    tc_forward(c, c.sched.tc_splits1, c.sched.tc_persistent, pred);
+  }
+  Scope sd(c.timers, "CG.tc_trans", true);
   tc_product(c, c.tcFt, c.map_yt_hi, c.map_yt_lo, M, c.sched.tc_splits, 0, 1.0f, c.hpart32.p, nullptr, nullptr, 0,
              pred, c.sched.tc_persistent);
 }
@@ -1189,18 +1270,22 @@ static int heuristic_tile(int R, int N, int nz = 1) {
 }
 
 // The FP32 Hessian row epilogue over hpart32's `parts` partials (row-
-// flattened where it applies); returns the number of p.Hp partials written.
+// flattened where it applies); returns the number of p.Hp partials written,
+// or 0 when the row-flattened form has already summed them into *vsum (its
+// last block, vsum != null).
 static int hvp_epilogue(Ctx& c, const float* p, const float* rs, const int8_t* ik, float* Hp, double* dpart,
-                        const double* pred, int parts) {
+                        const double* pred, int parts, double* vsum = nullptr) {
   const int M = (int)c.h.M, N = (int)c.h.N;
   const int RB = rows_per_block(N);
   if (RB > 0 && c.rows_option != 0) {
     const int threads = cdiv((int64_t)RB * N, 32) * 32;
+    const bool fused = vsum != nullptr && dpart != nullptr;
     k_hvp_epi32_rows<<<cdiv(M, RB), threads, 0, c.st>>>(c.hpart32.p, p, rs, c.maxr.p, rs ? 1 : 0,
                                                          (float)(2.0 * c.h.gam), ik, M, N, RB, Hp, dpart, pred,
-                                                         parts);
+                                                         parts, fused ? vsum : nullptr,
+                                                         fused ? c.counters.p + 4 : nullptr);
     post_launch(c);
-    return cdiv(M, RB);
+    return fused ? 0 : cdiv(M, RB);
   }
   const int tb = std::min(256, std::max(32, cdiv(N, 32) * 32));
   k_hvp_epi32<<<M, tb, 0, c.st>>>(c.hpart32.p, p, rs, c.maxr.p, rs ? 1 : 0, (float)(2.0 * c.h.gam), ik, M, N, Hp,
@@ -1229,9 +1314,10 @@ static void hvp32(Ctx& c, CGBufs<float>& b, const int8_t* ik, bool with_dot, con
     launch_band_gemm32(c, c.sched.trn_tile, c.tlo.p, c.tw.p, c.toff.p, c.tbval32.p, b.R2.p, M, N, 1.0f, c.hpart32.p,
                        pred, parts, 0, (int64_t)M * N, parts);
   }
+  Scope sd(c.timers, "CG.epilogue", true);
   const int nparts = hvp_epilogue(c, b.p.p, c.fullspace ? nullptr : b.rs.p, ik, b.Hp.p, with_dot ? c.part.p : nullptr,
-                                  pred, parts);
-  if (with_dot) reduce_to(c, c.part.p, nparts, c.sc.p + SC_V2, 1, false, 0.0, pred);
+                                  pred, parts, with_dot ? c.sc.p + SC_V2 : nullptr);
+  if (with_dot && nparts > 0) reduce_to(c, c.part.p, nparts, c.sc.p + SC_V2, 1, false, 0.0, pred);
 }
 
 // A chunk of CG iterations captured as a CUDA graph (on first use of its
@@ -1290,7 +1376,8 @@ static int cg_chunks(Ctx& c, std::array<uint64_t, 4> variant, Iter&& iteration) 
     const bool first = chunk_no == 0;
     const int chunk = first ? 4 : 8;
     if (c.use_graphs) {
-      CGGraph& gr = captured(c, {variant[0], variant[1], variant[2], variant[3], (uint64_t)first}, chunk, [&] {
+      const int spans = chunk * (c.timers.detail ? 8 : 1);  // timer spans recorded per chunk
+      CGGraph& gr = captured(c, {variant[0], variant[1], variant[2], variant[3], (uint64_t)first}, spans, [&] {
         for (int k = 0; k < chunk; ++k) iteration(first && k == 0);
       });
       CK(cudaGraphLaunch(gr.exec, c.st));
@@ -1310,13 +1397,14 @@ static int cg_chunks(Ctx& c, std::array<uint64_t, 4> variant, Iter&& iteration) 
 // The truncated-Newton PCG (2007-2090) in FP32 (mixed precision): the same
 // recurrence and exit test as cg_solve, tiled FP32 products, warp-per-row
 // lift, FP32 vectors with FP64 block sums.
-static void cg_solve32(Ctx& c, double bdfac) {
+// The FP32 CG's start (2007-2035): active set, r = -g, z, p, sn = 0, the
+// forcing term's scalars and the FP32 preconditioner.
+static void cg32_begin(Ctx& c, double bdfac) {
   const int M = (int)c.h.M, N = (int)c.h.N;
   const int64_t MN = (int64_t)M * N;
   const int g = elem_grid(MN);
   CGBufs<float>& b = c.cg32;
   require(c.tbval32.p, "F^T band values (FP32)");
-  Scope s(c.timers, "CG");
   k_cg_init<float><<<g, 256, 0, c.st>>>(c.X.p, c.G.p, c.bdiag.p, bdfac, kActiveTol, M, N, c.ik.p, b.r.p, b.z.p, b.p.p,
                                         b.sn.p, c.part.p, c.part2.p, c.ipart.p);
   post_launch(c);
@@ -1335,24 +1423,42 @@ static void cg_solve32(Ctx& c, double bdfac) {
     ListLine l;
     l.s("positivity constraints").i8(nact).s("active of").i8(MN).r8((double)nact / (double)MN).print();
   }
+}
+
+// The FP32 CG's end: its iteration count and (verbose) the reference's
+// newton-pcg lines.
+static void cg32_end(Ctx& c, int done_iters) {
+  c.n_cg += done_iters;
+  if (c.verbose) {
+    std::vector<double> lg(4 * kMaxCG);
+    CK(cudaMemcpyAsync(lg.data(), c.cglog.p, lg.size() * 8, cudaMemcpyDeviceToHost, c.st));
+    CK(cudaStreamSynchronize(c.st));
+    for (int j = 0; j < done_iters; ++j) {
+      ListLine l;
+      l.s("newton-pcg").i4(j + 1).s("sqrt(b2)=").r8(lg[4 * j]).s("eps=").r8(lg[4 * j + 1]).s("b1=").r8(lg[4 * j + 2]);
+      l.s("v2=").r8(lg[4 * j + 3]).print();
+    }
+  }
+}
+
+static void cg_solve32(Ctx& c, double bdfac) {
+  const int M = (int)c.h.M, N = (int)c.h.N;
+  const int64_t MN = (int64_t)M * N;
+  const int g = elem_grid(MN);
+  CGBufs<float>& b = c.cg32;
+  Scope s(c.timers, "CG");
+  cg32_begin(c, bdfac);
   const int lift_blocks = cdiv((int64_t)M * 32, 256);
+  const int gs = std::min(g, cdiv(M, 8));  // the step's blocks: 8 warps, one row per warp
   const bool tc = c.sched.tc != 0;
   auto iteration = [&](bool first) {
     if (tc) {
-      // p update (and reduced space: row sums), then the first product's
-      // operand split with BF's lift applied on the fly (no row-major V)
-      if (c.fullspace) {
-        if (!first) {
-          k_cg_pupdate<float><<<g, 256, 0, c.st>>>(c.sc.p, MN, b.p.p, b.z.p);
-          post_launch(c);
-        }
-      } else {
-        k_cg_lift32<<<lift_blocks, 256, 0, c.st>>>(first ? nullptr : c.sc.p, first ? 0 : 1, M, N, b.p.p, b.z.p,
-                                                   c.maxr.p, nullptr, b.rs.p);
-        post_launch(c);
-      }
-      k_split_t<<<dim3(cdiv(M, 32), cdiv(N, 32)), dim3(32, 8), 0, c.st>>>(
-          b.p.p, M, N, c.tc_mp, c.vt_hi.p, c.vt_lo.p, c.sc.p, c.fullspace ? nullptr : c.maxr.p, b.rs.p);
+      // p update, BF's lift (reduced space: row sums) and the first
+      // product's operand split in one launch (no row-major V)
+      Scope sd(c.timers, "CG.lift_split", true);
+      k_cg_lift_split<32><<<cdiv(M, 32), dim3(32, 32), 0, c.st>>>(c.sc.p, first ? 0 : 1, M, N, b.p.p, b.z.p,
+                                                              c.fullspace ? nullptr : c.maxr.p, b.rs.p, c.tc_mp,
+                                                              c.vt_hi.p, c.vt_lo.p);
       post_launch(c);
     } else if (c.fullspace) {
       if (!first) {
@@ -1368,23 +1474,15 @@ static void cg_solve32(Ctx& c, double bdfac) {
       Scope sb(c.timers, "BF");
       hvp32(c, b, c.ik.p, true, c.sc.p, tc);
     }
-    // the step; its last block sums r.z, r.r and advances the CG scalars
-    k_cg_step32<<<g, 256, 0, c.st>>>(c.sc.p, c.rsq32.p, M, N, b.p.p, b.Hp.p, b.sn.p, b.r.p, b.z.p, c.part.p,
-                                     c.part2.p, c.cglog.p, kMaxCG, c.counters.p + 1);
+    // the step (one warp per row); its last block sums r.z, r.r and
+    // advances the CG scalars
+    Scope sd(c.timers, "CG.step", true);
+    k_cg_step32<<<gs, 256, 0, c.st>>>(c.sc.p, c.rsq32.p, M, N, b.p.p, b.Hp.p, b.sn.p, b.r.p, b.z.p, c.part.p,
+                                      c.part2.p, c.cglog.p, kMaxCG, c.counters.p + 1);
     post_launch(c);
   };
   const int done_iters = cg_chunks(c, {0, (uint64_t)c.fullspace, 0, 0}, iteration);
-  c.n_cg += done_iters;
-  if (c.verbose) {
-    std::vector<double> lg(4 * kMaxCG);
-    CK(cudaMemcpyAsync(lg.data(), c.cglog.p, lg.size() * 8, cudaMemcpyDeviceToHost, c.st));
-    CK(cudaStreamSynchronize(c.st));
-    for (int j = 0; j < done_iters; ++j) {
-      ListLine l;
-      l.s("newton-pcg").i4(j + 1).s("sqrt(b2)=").r8(lg[4 * j]).s("eps=").r8(lg[4 * j + 1]).s("b1=").r8(lg[4 * j + 2]);
-      l.s("v2=").r8(lg[4 * j + 3]).print();
-    }
-  }
+  cg32_end(c, done_iters);
 }
 
 // ---------------------------------------------------------------------------
@@ -1771,6 +1869,55 @@ static double wall() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// Mode 2 (1953-2136), before the CG: the stage's space (stage 2: the max
+// column placeholder, 1970-1983) and the gradient.  Returns bdfac, the
+// preconditioner's factor of the space.
+static double outer_pre_cg(Ctx& c, int oiter) {
+  const int M = (int)c.h.M, N = (int)c.h.N;
+  c.fullspace = (oiter == 1);
+  if (!c.fullspace) {
+    k_stage2_start_t<<<cdiv(M, 32), kTileThreads, 0, c.st>>>(c.X.p, c.maxr.p, M, N, 1);
+    post_launch(c);
+    if (c.exact) {
+      touch_x(c);
+    } else {
+      // mixed path: the placeholder is replaced by the next rebuild, which
+      // restores X to within ulps; only the reduced gradient (new maxr)
+      // must be derived again
+      c.G_ver = -1;
+    }
+  } else {
+    set_full_space(c);
+  }
+  op_dL(c);
+  if (c.precision == PQDTS_MIXED && c.refine_option == 1 && !c.fullspace) c.refine = true;
+  return c.fullspace ? 1.0 : 2.0;
+}
+
+// Whether this iteration's CG runs in FP32 (the mixed solver before its
+// final refinement).
+static bool cg_in_fp32(const Ctx& c) { return c.precision == PQDTS_MIXED && !c.refine; }
+
+// Mode 2 after the CG: the two-metric direction (2092-2104) and the line
+// search; the mixed solver switches to its FP64 refinement once an FP32
+// Newton direction stops giving progress in stage 2.
+static void outer_post_cg(Ctx& c, SolveState& st, double bdfac, bool fp32) {
+  const int M = (int)c.h.M, N = (int)c.h.N;
+  const int g = elem_grid((int64_t)M * N);
+  if (c.precision == PQDTS_MIXED && c.refine) c.n_refine++;
+  op_dL(c);
+  const int32_t* mr = c.fullspace ? nullptr : c.maxr.p;
+  if (fp32) k_twometric<float><<<g, 256, 0, c.st>>>(c.cg32.sn.p, c.G.p, c.ik.p, mr, c.bdiag.p, bdfac, M, N, c.sn64.p);
+  else k_twometric<double><<<g, 256, 0, c.st>>>(c.cg64.sn.p, c.G.p, c.ik.p, mr, c.bdiag.p, bdfac, M, N, c.sn64.p);
+  post_launch(c);
+  if (c.exact) line_search(c, !c.fullspace, st.alpha, st.dlalpha);
+  else line_search_mixed(c, !c.fullspace, st.alpha, st.dlalpha);
+  if (c.precision == PQDTS_MIXED && !c.refine && !c.fullspace && (st.alpha == 0.0 || st.dlalpha >= 0.0))
+    c.refine = true;
+}
+
+static void outer_tail(Ctx& c, SolveState& st);
+
 // One outer iteration of mode 2 (1953-2136) or mode 1 (1934-1951, 2111-2136).
 static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
   const int M = (int)c.h.M, N = (int)c.h.N;
@@ -1786,40 +1933,22 @@ static void outer_iteration(Ctx& c, int mode, int oiter, SolveState& st) {
     post_launch(c);
     line_search(c, true, st.alpha, st.dlalpha);
   } else {
-    c.fullspace = (oiter == 1);
-    if (!c.fullspace) {
-      k_stage2_start_t<<<cdiv(M, 32), kTileThreads, 0, c.st>>>(c.X.p, c.maxr.p, M, N, 1);
-      post_launch(c);
-      if (c.exact) {
-        touch_x(c);
-      } else {
-        // mixed path: the placeholder is replaced by the next rebuild, which
-        // restores X to within ulps; only the reduced gradient (new maxr)
-        // must be derived again
-        c.G_ver = -1;
-      }
-    } else {
-      set_full_space(c);
-    }
-    op_dL(c);
-    const double bdfac = c.fullspace ? 1.0 : 2.0;
-    if (c.precision == PQDTS_MIXED && c.refine_option == 1 && !c.fullspace) c.refine = true;
-    const bool fp32 = (c.precision == PQDTS_MIXED) && !c.refine;
+    const double bdfac = outer_pre_cg(c, oiter);
+    const bool fp32 = cg_in_fp32(c);
     if (fp32) cg_solve32(c, bdfac);
     else cg_solve<double>(c, c.cg64, c.fval.p, c.tval.p, bdfac, nullptr);
-    if (c.precision == PQDTS_MIXED && c.refine) c.n_refine++;
-    op_dL(c);
-    const int32_t* mr = c.fullspace ? nullptr : c.maxr.p;
-    if (fp32) k_twometric<float><<<g, 256, 0, c.st>>>(c.cg32.sn.p, c.G.p, c.ik.p, mr, c.bdiag.p, bdfac, M, N, c.sn64.p);
-    else k_twometric<double><<<g, 256, 0, c.st>>>(c.cg64.sn.p, c.G.p, c.ik.p, mr, c.bdiag.p, bdfac, M, N, c.sn64.p);
-    post_launch(c);
-    if (c.exact) line_search(c, !c.fullspace, st.alpha, st.dlalpha);
-    else line_search_mixed(c, !c.fullspace, st.alpha, st.dlalpha);
-    // Mixed precision: once the FP32 Newton direction stops giving progress
-    // the remaining iterations run the CG in FP64 (final refinement).
-    if (c.precision == PQDTS_MIXED && !c.refine && !c.fullspace && (st.alpha == 0.0 || st.dlalpha >= 0.0))
-      c.refine = true;
+    outer_post_cg(c, st, bdfac, fp32);
   }
+  outer_tail(c, st);
+}
+
+// The end of an outer iteration (2111-2136): the update X + alpha s and its
+// projection (or, mixed path, the adopted line-search candidate), then L,
+// dL, |der| and conv_test.
+static void outer_tail(Ctx& c, SolveState& st) {
+  const int M = (int)c.h.M, N = (int)c.h.N;
+  const int64_t MN = (int64_t)M * N;
+  const int g = elem_grid(MN);
   // Mixed path: the chosen step was evaluated to FP64 accuracy as a
   // line-search candidate (projected, rebuilt, its residual and objective known): adopt
   // it instead of recomputing the same projection and banded product.
@@ -1971,24 +2100,29 @@ static void nonneg_x(Ctx& c, SolveState& st) {
   st.L0 = op_L(c);
 }
 
-static void solve(Ctx& c, int mode, int maxiiter, double conv_thres, int start_stage, int output, pqdts_stage_cb cb,
-                  void* user, double* stats) {
-  need_problem(c);
-  if (mode != 1 && mode != 2) throw Err(PQDTS_E_ARG, "mode must be 1 or 2");
-  if (start_stage < 1 || start_stage > 2) throw Err(PQDTS_E_ARG, "start_stage must be 1 or 2");
-  SolveState st;
+// The start of a solve (1908-1915): counters, the seeded first maxr, the
+// objective and gradient of the starting point (full space) and |der|^2.
+static void solve_prologue(Ctx& c, SolveState& st) {
   c.n_cg = c.n_lsL = c.n_refine = 0;
   c.refine = false;
   CK(cudaMemcpyAsync(c.maxr.p, c.h_maxr.data(), c.h.M * 4, cudaMemcpyHostToDevice, c.st));
   c.h2d += c.h.M * 4;
   touch_x(c);
-  // 1908-1915: objective and gradient of the starting point (full space).
   c.fullspace = true;
   st.L0 = op_L(c);
   op_dL(c);
   dot_dev(c, c.G.p, c.G.p, c.sc.p + SC_TMP);
   read_back(c, c.sc.p + SC_TMP, 1);
   st.norm_der = c.pin[0];
+}
+
+static void solve(Ctx& c, int mode, int maxiiter, double conv_thres, int start_stage, int output, pqdts_stage_cb cb,
+                  void* user, double* stats) {
+  need_problem(c);
+  if (mode != 1 && mode != 2) throw Err(PQDTS_E_ARG, "mode must be 1 or 2");
+  if (start_stage < 1 || start_stage > 2) throw Err(PQDTS_E_ARG, "start_stage must be 1 or 2");
+  SolveState st;
+  solve_prologue(c, st);
   if (c.verbose) {
     ListLine l;
     l.s("iter").i4(0).i4(0).s("L=").r8(st.L0).s("||der||=").r8(std::sqrt(st.norm_der)).s("dt=").r8(0.0).s("ttot=").r8(0.0);
@@ -2011,6 +2145,180 @@ static void solve(Ctx& c, int mode, int maxiiter, double conv_thres, int start_s
   c.timers.flush();
   CK(cudaStreamSynchronize(c.st));
   fill_stats(c, st, wall() - t0, stats);
+}
+
+// ---------------------------------------------------------------------------
+// Lockstep solve of a group of mixed-precision instances that share F (the
+// resampled / gamma-swept members of a batch).  Each member is a context of
+// its own (its P, gamma, iterate, line search, stages), all on the group
+// context's stream; in every round each member runs up to its CG (stage
+// logic and gradient), the members whose CG is in FP32 then run it jointly
+// -- one launch per CG phase for all of them, the tensor-core products over
+// the group context's widened problem (M, G*N, D: the members' V side by
+// side; batch_cg.cuh) -- and each member finishes its outer iteration (line
+// search, update, conv_test).  A member's arithmetic is the single-instance
+// solver's; its stage and stopping logic is run_stage / solve's, as a state
+// machine (mode 2, no stage callback, no printing).
+// ---------------------------------------------------------------------------
+struct MemberRun {
+  Ctx* c = nullptr;
+  SolveState st;
+  int oiter = 1, iiter = 0;
+  bool in_stage = false, finished = false, stepped = false, fp32 = false;
+  double bdfac = 1.0, t0 = 0.0;
+  int maxiiter = 0;
+  double conv_thres = 0.0;
+  double* stats = nullptr;
+};
+
+static void member_end_stage(MemberRun& m) {
+  Ctx& c = *m.c;
+  m.st.conv = op_conv(c, false);
+  c.timers.flush();
+  if (c.precision == PQDTS_MIXED) nonneg_x(c, m.st);
+  m.in_stage = false;
+  m.oiter++;
+}
+
+// Runs the member up to its next CG (run_stage's loop head and the outer
+// iteration's first part); false once its solve has finished.
+static bool member_next(MemberRun& m) {
+  Ctx& c = *m.c;
+  for (;;) {
+    if (m.finished) return false;
+    if (!m.in_stage) {
+      if (m.oiter > 2 || c.target_hit) {
+        CK(cudaStreamSynchronize(c.st));
+        fill_stats(c, m.st, wall() - m.t0, m.stats);
+        m.finished = true;
+        return false;
+      }
+      m.st.dlalpha = -kHuge;
+      m.iiter = 0;
+      m.in_stage = true;
+    }
+    const bool stage1_exit = m.oiter == 1 && (std::fabs(m.st.dlalpha) < kStage1Exit || m.st.dlalpha > 0);
+    if (m.iiter >= m.maxiiter || stage1_exit) {
+      member_end_stage(m);
+      continue;
+    }
+    m.iiter++;
+    m.bdfac = outer_pre_cg(c, m.oiter);
+    m.fp32 = cg_in_fp32(c);
+    return true;
+  }
+}
+
+// The rest of the member's outer iteration and run_stage's exit tests.
+static void member_after_cg(MemberRun& m) {
+  Ctx& c = *m.c;
+  outer_post_cg(c, m.st, m.bdfac, m.fp32);
+  outer_tail(c, m.st);
+  if (m.st.conv < m.conv_thres) {
+    member_end_stage(m);
+  } else if (c.target_L > 0 && m.st.L0 <= c.target_L) {
+    c.target_hit = true;
+    member_end_stage(m);
+  }
+}
+
+// The FP32 CG of the members listed in `in_cg` (their cg32_begin queued),
+// one launch per phase for all of them on g's stream.
+static void group_cg32(Ctx& g, std::vector<MemberRun>& ms, const std::vector<int>& in_cg) {
+  const int G = (int)ms.size();
+  const int M = (int)g.h.M, N = (int)ms[0].c->h.N;
+  const int64_t Nw = g.h.N;  // G * N
+  g.h_memtab.assign(G, CGMember{});
+  for (int j : in_cg) {
+    Ctx& c = *ms[j].c;
+    CGMember& e = g.h_memtab[j];
+    e.p = c.cg32.p.p;
+    e.z = c.cg32.z.p;
+    e.rs = c.cg32.rs.p;
+    e.Hp = c.cg32.Hp.p;
+    e.sn = c.cg32.sn.p;
+    e.r = c.cg32.r.p;
+    e.rsq = c.rsq32.p;
+    e.maxr = c.fullspace ? nullptr : c.maxr.p;
+    e.ik = c.ik.p;
+    e.sc = c.sc.p;
+    e.part_rz = c.part.p;
+    e.part_rr = c.part2.p;
+    e.dpart = c.part.p;
+    e.cnt_epi = c.counters.p + 4;
+    e.cnt_step = c.counters.p + 1;
+    e.log = c.cglog.p;
+    e.c2gam = (float)(2.0 * c.h.gam);
+    e.active = 1;
+  }
+  g.memtab.alloc(G);
+  CK(cudaMemcpyAsync(g.memtab.p, g.h_memtab.data(), G * sizeof(CGMember), cudaMemcpyHostToDevice, g.st));
+  CK(cudaMemsetAsync(g.counters.p + 6, 0, sizeof(unsigned), g.st));
+  CK(cudaMemsetAsync(g.sc.p + SC_DONE, 0, sizeof(double), g.st));
+  const int active = (int)in_cg.size();
+  const CGGroup grp{g.counters.p + 6, g.sc.p, active};
+  const int RB = rows_per_block(N);
+  const int rthreads = cdiv((int64_t)RB * N, 32) * 32;
+  const int gs = std::min(elem_grid((int64_t)M * N), cdiv(M, 8));
+  auto iteration = [&](bool first) {
+    k_cg_lift_split_b<32><<<dim3(cdiv(M, 32), G), dim3(32, 32), 0, g.st>>>(g.memtab.p, first ? 0 : 1, M, N, g.tc_mp,
+                                                                           g.vt_hi.p, g.vt_lo.p);
+    post_launch(g);
+    tc_forward(g, g.sched.tc_splits1, g.sched.tc_persistent, g.sc.p);
+    tc_product(g, g.tcFt, g.map_yt_hi, g.map_yt_lo, M, g.sched.tc_splits, 0, 1.0f, g.hpart32.p, nullptr, nullptr, 0,
+               g.sc.p, g.sched.tc_persistent);
+    k_hvp_epi32_rows_b<<<dim3(cdiv(M, RB), G), rthreads, 0, g.st>>>(g.memtab.p, g.hpart32.p, Nw, (int64_t)M * Nw, M,
+                                                                     N, RB, g.sched.tc_splits);
+    post_launch(g);
+    k_cg_step32_b<<<dim3(gs, G), 256, 0, g.st>>>(g.memtab.p, grp, M, N, kMaxCG);
+    post_launch(g);
+  };
+  cg_chunks(g, {100, (uint64_t)active, 0, 0}, iteration);
+  for (int j : in_cg) {
+    Ctx& c = *ms[j].c;
+    read_back(c, c.sc.p, SC_NSC);
+    cg32_end(c, (int)c.pin[SC_ITER]);
+  }
+}
+
+// Whether a group of `members` instances of this shape can take the joint
+// CG: tensor-core products on the group context and the row-flattened
+// epilogue (32 <= N <= 1024).
+static bool group_ready(const Ctx& g, int64_t N) {
+  return g.have_problem && g.precision == PQDTS_MIXED && g.sched.tc && g.tc_ready && rows_per_block((int)N) > 0 &&
+         g.rows_option != 0;
+}
+
+static void group_solve(Ctx& g, std::vector<MemberRun>& ms) {
+  for (MemberRun& m : ms) {
+    Ctx& c = *m.c;
+    need_problem(c);
+    solve_prologue(c, m.st);
+    m.t0 = wall();
+    m.st.t0 = m.t0;
+    c.target_hit = false;
+  }
+  std::vector<int> in_cg;
+  for (;;) {
+    in_cg.clear();
+    bool any = false;
+    for (int j = 0; j < (int)ms.size(); ++j) {
+      MemberRun& m = ms[j];
+      m.stepped = member_next(m);
+      if (!m.stepped) continue;
+      any = true;
+      if (m.fp32) {
+        cg32_begin(*m.c, m.bdfac);
+        in_cg.push_back(j);
+      } else {  // the member's FP64 refinement CG, on its own
+        cg_solve<double>(*m.c, m.c->cg64, m.c->fval.p, m.c->tval.p, m.bdfac, nullptr);
+      }
+    }
+    if (!any) break;
+    if (!in_cg.empty()) group_cg32(g, ms, in_cg);
+    for (MemberRun& m : ms)
+      if (m.stepped) member_after_cg(m);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -2281,6 +2589,10 @@ static void choose_schedule(Ctx& c) {
     s.trans_rows = c.rows_option && c.t_contiguous ? 1 : 0;
   }
   c.sched = s;
+  if (s.tc && s.tc_persistent) {  // tile lists of the persistent kernel, built before any capture
+    tc_sched(c, c.tcF, c.tc_bn, std::max(1, s.tc_splits1));
+    tc_sched(c, c.tcFt, c.tc_bn, s.tc_splits);
+  }
   if (s.tc && s.tc_splits1 > 1) {
     const size_t need1 = (size_t)s.tc_splits1 * (size_t)h.D * (size_t)h.N;
     if (c.ypart.n != need1) c.ypart.alloc(need1);
@@ -2295,6 +2607,36 @@ static void choose_schedule(Ctx& c) {
   }
   read_back(c, c.sc.p, SC_NSC);
   check_tc_error(c);
+}
+
+// Internal F (pqdts.f90:1366-1466) computed on the device: each probe row's
+// window (k_internal_windows, one thread per row scanning as the reference
+// does) and its values (k_internal_values); the host then builds the
+// transposed CSR and the Hessian diagonal from them as from any band input.
+static void bands_internal_device(Ctx& c, HostProblem& h) {
+  if (h.M != (h.D - 1) * (h.D - 1)) throw std::invalid_argument("M is not (D-1)**2");
+  const int D = (int)h.D;
+  const double sqrt_2pi = std::sqrt(2 * (4.0 * std::atan(1.0)));  // as the host fprob
+  DBuf<int32_t> lo, w;
+  DBuf<int64_t> off;
+  DBuf<double> val;
+  lo.alloc(D);
+  w.alloc(D);
+  k_internal_windows<<<cdiv(D, 128), 128, 0, c.st>>>(h.M, D, sqrt_2pi, lo.p, w.p);
+  post_launch(c);
+  h.flo.assign(D, -1);
+  h.fw.assign(D, 0);
+  CK(cudaMemcpyAsync(h.flo.data(), lo.p, (size_t)D * 4, cudaMemcpyDeviceToHost, c.st));
+  CK(cudaMemcpyAsync(h.fw.data(), w.p, (size_t)D * 4, cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+  finish_offsets(h);
+  if (h.fval.empty()) return;
+  off.upload(h.foff.data(), D, c.st, nullptr);
+  val.alloc(h.fval.size());
+  k_internal_values<<<D, 256, 0, c.st>>>(D, sqrt_2pi, lo.p, w.p, off.p, val.p);
+  post_launch(c);
+  CK(cudaMemcpyAsync(h.fval.data(), val.p, h.fval.size() * 8, cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
 }
 
 // Problem set-up shared by the entry points.
@@ -2358,7 +2700,9 @@ static int guarded(Ctx* c, F&& f) {
 
 extern "C" {
 
-int pqdts_cuda_create(int32_t device, pqdts_ctx** out) {
+// A context on `device`, with its own stream or (shared != null, the
+// members of a batched group) on another context's stream.
+static int create_ctx(int32_t device, cudaStream_t shared, pqdts_ctx** out) {
   if (!out) return PQDTS_E_ARG;
   *out = nullptr;
   Ctx* c = new (std::nothrow) Ctx();
@@ -2369,13 +2713,18 @@ int pqdts_cuda_create(int32_t device, pqdts_ctx** out) {
     CK(cudaGetDeviceCount(&n));
     if (device < 0 || device >= n) throw Err(PQDTS_E_ARG, "no CUDA device " + std::to_string(device));
     CK(cudaSetDevice(device));
-    CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    if (shared) {
+      c->st = shared;
+      c->own_stream = false;
+    } else {
+      CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    }
     CK(cudaMallocHost((void**)&c->pin, 64 * sizeof(double)));
     c->timers.st = c->st;
   });
   if (rc != PQDTS_OK) {
     fprintf(stderr, "pqdts_cuda_create: %s\n", c->err.c_str());
-    if (c->st) cudaStreamDestroy(c->st);
+    if (c->st && c->own_stream) cudaStreamDestroy(c->st);
     delete c;
     return rc;
   }
@@ -2383,12 +2732,14 @@ int pqdts_cuda_create(int32_t device, pqdts_ctx** out) {
   return PQDTS_OK;
 }
 
+int pqdts_cuda_create(int32_t device, pqdts_ctx** out) { return create_ctx(device, nullptr, out); }
+
 int pqdts_cuda_destroy(pqdts_ctx* c) {
   if (!c) return PQDTS_E_ARG;
   cudaSetDevice(c->device);
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->pin) cudaFreeHost(c->pin);
-  cudaStream_t st = c->st;
+  cudaStream_t st = c->own_stream ? c->st : nullptr;
   delete c;
   if (st) cudaStreamDestroy(st);
   return PQDTS_OK;
@@ -2446,6 +2797,8 @@ int pqdts_cuda_set_problem_coo(pqdts_ctx* c, int64_t M, int64_t N, int64_t D, in
     if (nnzF >= 0) {
       if (nnzF > 0 && (!Fr || !Fc || !Fv)) throw Err(PQDTS_E_ARG, "null F arrays");
       pqdts::bands_from_coo(h, nnzF, Fr, Fc, Fv);
+    } else if (c->internal_f_option == 1 || (c->internal_f_option < 0 && precision == PQDTS_MIXED)) {
+      pqdts::bands_internal_device(*c, h);
     } else {
       pqdts::bands_internal(h);
     }
@@ -2842,7 +3195,10 @@ int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
     } else if (n == "autotune") {
       c->autotune = value != 0;
     } else if (n == "timers") {
+      if (value < 0 || value > 2) throw pqdts::Err(PQDTS_E_ARG, "timers must be 0, 1 or 2");
       c->timers.enabled = value != 0;
+      c->timers.detail = value == 2;
+      c->drop_graphs();  // captured CG chunks carry their timer spans
     } else if (n == "rows_kernels") {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "rows_kernels must be -1, 0 or 1");
       c->rows_option = (int)value;
@@ -2858,6 +3214,9 @@ int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
     } else if (n == "df_products") {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "df_products must be -1, 0 or 1");
       c->df_option = (int)value;
+    } else if (n == "internal_f") {
+      if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "internal_f must be -1, 0 or 1");
+      c->internal_f_option = (int)value;
     } else if (n == "fp64_refine") {
       if (value < 0 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "fp64_refine must be 0 or 1");
       c->refine_option = (int)value;
@@ -2886,7 +3245,7 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     const pqdts::Schedule& s = c->sched;
     if (n == "graphs") *value = c->use_graphs;
     else if (n == "autotune") *value = c->autotune;
-    else if (n == "timers") *value = c->timers.enabled;
+    else if (n == "timers") *value = c->timers.enabled ? (c->timers.detail ? 2 : 1) : 0;
     else if (n == "sched.fwd_tile") *value = s.fwd_tile;
     else if (n == "sched.trn_tile") *value = s.trn_tile;
     else if (n == "sched.trn_splits") *value = s.trn_splits;
@@ -2908,6 +3267,7 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     else if (n == "tc_wait_ms") *value = (int64_t)(c->tc_wait_ns / 1000000ull);
     else if (n == "tc_wait_probe") *value = c->tc_wait_probe;
     else if (n == "fp64_refine") *value = c->refine_option;
+    else if (n == "internal_f") *value = c->internal_f_option;
     else if (n == "sched.df_fwd") *value = c->df_fwd;
     else if (n == "sched.df_trans") *value = c->df_trans;
     else if (n == "graphs.captured") *value = (int64_t)c->graphs.size();
@@ -2929,6 +3289,98 @@ int pqdts_cuda_timer(pqdts_ctx* c, const char* name, double* seconds, int64_t* c
   });
 }
 
+// Tasks of a batched solve: single instances, and groups of instances that
+// share F (the same M, N, D and bands and values) solved in lockstep with a
+// joint CG (mixed precision, mode 2, 32 <= N <= 1024; at most kGroupMax
+// members and M*G*N < 2^31 per group).  PQDTS_BATCH_GROUPS=0 turns the
+// grouping off.
+static constexpr int kGroupMax = 16;
+
+static std::vector<std::vector<int>> batch_tasks(int n_inst, const int64_t* M, const int64_t* N, const int64_t* D,
+                                                 const int64_t* band_lo, const int64_t* band_hi,
+                                                 const double* band_vals, const int64_t* band_row_offset,
+                                                 const int64_t* band_val_offset, bool grouping) {
+  std::vector<std::vector<int>> tasks;
+  if (!grouping) {
+    for (int k = 0; k < n_inst; ++k) tasks.push_back({k});
+    return tasks;
+  }
+  auto nvals = [&](int k) {
+    int64_t t = 0;
+    for (int64_t d = 0; d < D[k]; ++d)
+      if (band_lo[band_row_offset[k] + d] >= 0) t += band_hi[band_row_offset[k] + d] - band_lo[band_row_offset[k] + d] + 1;
+    return t;
+  };
+  auto fnv = [](uint64_t h, const void* p, size_t n) {
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 0x100000001B3ULL;
+    return h;
+  };
+  std::vector<int64_t> nv(n_inst);
+  std::map<uint64_t, std::vector<int>> buckets;
+  std::vector<uint64_t> key(n_inst);
+  for (int k = 0; k < n_inst; ++k) {
+    nv[k] = nvals(k);
+    uint64_t h = 0xCBF29CE484222325ULL;
+    const int64_t shape[4] = {M[k], N[k], D[k], nv[k]};
+    h = fnv(h, shape, sizeof(shape));
+    h = fnv(h, band_lo + band_row_offset[k], (size_t)D[k] * 8);
+    h = fnv(h, band_hi + band_row_offset[k], (size_t)D[k] * 8);
+    h = fnv(h, band_vals + band_val_offset[k], (size_t)nv[k] * 8);
+    key[k] = h;
+    buckets[h].push_back(k);
+  }
+  auto same = [&](int a, int b) {
+    return M[a] == M[b] && N[a] == N[b] && D[a] == D[b] && nv[a] == nv[b] &&
+           std::memcmp(band_lo + band_row_offset[a], band_lo + band_row_offset[b], (size_t)D[a] * 8) == 0 &&
+           std::memcmp(band_hi + band_row_offset[a], band_hi + band_row_offset[b], (size_t)D[a] * 8) == 0 &&
+           std::memcmp(band_vals + band_val_offset[a], band_vals + band_val_offset[b], (size_t)nv[a] * 8) == 0;
+  };
+  std::vector<char> taken(n_inst, 0);
+  for (int k = 0; k < n_inst; ++k) {
+    if (taken[k]) continue;
+    std::vector<int> grp{k};
+    taken[k] = 1;
+    for (int j : buckets[key[k]])
+      if (!taken[j] && same(k, j)) {
+        grp.push_back(j);
+        taken[j] = 1;
+      }
+    const int64_t cap = std::max<int64_t>(1, std::min<int64_t>(kGroupMax, (((int64_t)1 << 31) - 1) / (M[k] * N[k])));
+    const bool joint = grp.size() >= 2 && N[k] >= 32 && N[k] <= 1024 && cap >= 2;
+    if (!joint) {
+      for (int j : grp) tasks.push_back({j});
+      continue;
+    }
+    // equal parts of at most `cap` members
+    const int64_t parts = ((int64_t)grp.size() + cap - 1) / cap;
+    size_t at = 0;
+    for (int64_t q = 0; q < parts; ++q) {
+      const size_t n = (grp.size() - at) / (size_t)(parts - q);
+      tasks.emplace_back(grp.begin() + at, grp.begin() + at + n);
+      at += n;
+    }
+  }
+  return tasks;
+}
+
+int pqdts_cuda_batch_groups(int32_t n_inst, const int64_t* M, const int64_t* N, const int64_t* D,
+                            const int64_t* band_lo, const int64_t* band_hi, const double* band_vals,
+                            const int64_t* band_row_offset, const int64_t* band_val_offset, int32_t* group_of) {
+  if (n_inst <= 0 || !M || !N || !D || !band_lo || !band_hi || !band_vals || !band_row_offset || !band_val_offset ||
+      !group_of)
+    return PQDTS_E_ARG;
+  try {
+    const auto tasks = batch_tasks(n_inst, M, N, D, band_lo, band_hi, band_vals, band_row_offset, band_val_offset, true);
+    for (size_t t = 0; t < tasks.size(); ++t)
+      for (int k : tasks[t]) group_of[k] = tasks[t].size() >= 2 ? (int32_t)t : -1;
+  } catch (const std::exception& e) {
+    fprintf(stderr, "pqdts_cuda_batch_groups: %s\n", e.what());
+    return PQDTS_E_STATE;
+  }
+  return PQDTS_OK;
+}
+
 int pqdts_cuda_solve_batch(int32_t device, int32_t n_inst, const int64_t* M, const int64_t* N, const int64_t* D,
                            const int64_t* band_lo, const int64_t* band_hi, const double* band_vals,
                            const int64_t* band_row_offset, const int64_t* band_val_offset, const double* P,
@@ -2938,18 +3390,99 @@ int pqdts_cuda_solve_batch(int32_t device, int32_t n_inst, const int64_t* M, con
   if (n_inst <= 0 || !M || !N || !D || !band_lo || !band_hi || !band_vals || !band_row_offset || !band_val_offset ||
       !P || !P_offset || !gamma || !X)
     return PQDTS_E_ARG;
-  // Instances are independent: a pool of host workers, each with its own
-  // context and stream, so the instances' kernels overlap on the device.
+  // Tasks are independent: a pool of host workers, each with its own
+  // context and stream, so the tasks' kernels overlap on the device.
   std::vector<int64_t> xoff(n_inst + 1, 0);
   for (int k = 0; k < n_inst; ++k) xoff[k + 1] = xoff[k] + M[k] * N[k];
+  bool grouping = precision == PQDTS_MIXED && mode == 2;
+  if (const char* e = std::getenv("PQDTS_BATCH_GROUPS")) grouping = grouping && std::atoi(e) != 0;
+  std::vector<std::vector<int>> tasks;
+  try {
+    tasks = batch_tasks(n_inst, M, N, D, band_lo, band_hi, band_vals, band_row_offset, band_val_offset, grouping);
+  } catch (const std::exception& e) {
+    fprintf(stderr, "pqdts_cuda_solve_batch: %s\n", e.what());
+    return PQDTS_E_STATE;
+  }
+  const int ntask = (int)tasks.size();
   // workers: PQDTS_BATCH_WORKERS (default: the host's hardware threads, at
-  // most 16), at most one per instance
+  // most 16), at most one per task
   int workers = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
   if (const char* e = std::getenv("PQDTS_BATCH_WORKERS")) workers = std::max(1, std::min(64, std::atoi(e)));
-  workers = std::min<int>(n_inst, workers);
+  workers = std::min<int>(ntask, workers);
   std::atomic<int> next{0};
   std::atomic<int> rc{PQDTS_OK};
   std::mutex err_mu;
+  auto fail = [&](int k, pqdts_ctx* c, int r) {
+    std::lock_guard<std::mutex> g(err_mu);
+    fprintf(stderr, "pqdts_cuda_solve_batch: instance %d: %s\n", k, c ? c->err.c_str() : "context creation failed");
+    rc = r;
+  };
+  auto setup = [&](pqdts_ctx* c, int k) {
+    const int64_t* lo = band_lo + band_row_offset[k];
+    const int64_t* hi = band_hi + band_row_offset[k];
+    int r = pqdts_cuda_set_problem(c, M[k], N[k], D[k], lo, hi, band_vals + band_val_offset[k], P + P_offset[k],
+                                   gamma[k], precision);
+    if (r == PQDTS_OK) r = pqdts_cuda_set_x(c, X + xoff[k]);
+    if (r == PQDTS_OK) r = pqdts_cuda_set_objective_target(c, target_L ? target_L[k] : 0.0);
+    return r;
+  };
+  auto single = [&](pqdts_ctx* c, int k) {
+    int r = setup(c, k);
+    if (r == PQDTS_OK)
+      r = pqdts_cuda_solve(c, mode, maxiiter, conv_thres, 1, 0, nullptr, nullptr,
+                           stats ? stats + (int64_t)k * PQDTS_NSTATS : nullptr);
+    if (r == PQDTS_OK) r = pqdts_cuda_get_x(c, X + xoff[k]);
+    if (r != PQDTS_OK) fail(k, c, r);
+  };
+  // A group: the widened problem (M, G*N, D, the shared F; P and gamma are
+  // not used) on a group context whose stream the members share; members
+  // fall back to single solves when the group cannot take the joint CG.
+  auto group = [&](pqdts_ctx* c, const std::vector<int>& ks) {
+    const int G = (int)ks.size(), k0 = ks[0];
+    pqdts_ctx* g = nullptr;
+    int r = pqdts_cuda_create(device, &g);
+    if (r == PQDTS_OK) {
+      g->timers.enabled = false;
+      std::vector<double> Pz((size_t)D[k0] * N[k0] * G, 0.0);
+      r = pqdts_cuda_set_problem(g, M[k0], N[k0] * G, D[k0], band_lo + band_row_offset[k0],
+                                 band_hi + band_row_offset[k0], band_vals + band_val_offset[k0], Pz.data(), 0.0,
+                                 precision);
+    }
+    if (r != PQDTS_OK || !pqdts::group_ready(*g, N[k0])) {
+      if (g) pqdts_cuda_destroy(g);
+      for (int k : ks)
+        if (rc.load() == PQDTS_OK) single(c, k);
+      return;
+    }
+    std::vector<pqdts_ctx*> mc(G, nullptr);
+    std::vector<pqdts::MemberRun> ms(G);
+    for (int j = 0; j < G && r == PQDTS_OK; ++j) {
+      r = create_ctx(device, g->st, &mc[j]);
+      if (r != PQDTS_OK) {
+        fail(ks[j], nullptr, r);
+        break;
+      }
+      mc[j]->timers.enabled = false;
+      mc[j]->tc_option = 0;  // the members' own CG products are not used
+      r = setup(mc[j], ks[j]);
+      if (r != PQDTS_OK) fail(ks[j], mc[j], r);
+      ms[j].c = mc[j];
+      ms[j].maxiiter = maxiiter;
+      ms[j].conv_thres = conv_thres;
+      ms[j].stats = stats ? stats + (int64_t)ks[j] * PQDTS_NSTATS : nullptr;
+    }
+    if (r == PQDTS_OK) {
+      r = guarded(g, [&] { pqdts::group_solve(*g, ms); });
+      if (r != PQDTS_OK) fail(k0, g, r);
+    }
+    for (int j = 0; j < G && r == PQDTS_OK; ++j) {
+      r = pqdts_cuda_get_x(mc[j], X + xoff[ks[j]]);
+      if (r != PQDTS_OK) fail(ks[j], mc[j], r);
+    }
+    for (pqdts_ctx* m : mc)
+      if (m) pqdts_cuda_destroy(m);
+    pqdts_cuda_destroy(g);
+  };
   auto work = [&]() {
     pqdts_ctx* c = nullptr;
     int r = pqdts_cuda_create(device, &c);
@@ -2959,23 +3492,10 @@ int pqdts_cuda_solve_batch(int32_t device, int32_t n_inst, const int64_t* M, con
     }
     c->timers.enabled = false;  // no per-region events in the batch
     for (;;) {
-      const int k = next++;
-      if (k >= n_inst || rc.load() != PQDTS_OK) break;
-      const int64_t* lo = band_lo + band_row_offset[k];
-      const int64_t* hi = band_hi + band_row_offset[k];
-      r = pqdts_cuda_set_problem(c, M[k], N[k], D[k], lo, hi, band_vals + band_val_offset[k], P + P_offset[k],
-                                 gamma[k], precision);
-      if (r == PQDTS_OK) r = pqdts_cuda_set_x(c, X + xoff[k]);
-      if (r == PQDTS_OK) r = pqdts_cuda_set_objective_target(c, target_L ? target_L[k] : 0.0);
-      if (r == PQDTS_OK)
-        r = pqdts_cuda_solve(c, mode, maxiiter, conv_thres, 1, 0, nullptr, nullptr,
-                             stats ? stats + (int64_t)k * PQDTS_NSTATS : nullptr);
-      if (r == PQDTS_OK) r = pqdts_cuda_get_x(c, X + xoff[k]);
-      if (r != PQDTS_OK) {
-        std::lock_guard<std::mutex> g(err_mu);
-        fprintf(stderr, "pqdts_cuda_solve_batch: instance %d: %s\n", k, c->err.c_str());
-        rc = r;
-      }
+      const int t = next++;
+      if (t >= ntask || rc.load() != PQDTS_OK) break;
+      if (tasks[t].size() == 1) single(c, tasks[t][0]);
+      else group(c, tasks[t]);
     }
     pqdts_cuda_destroy(c);
   };

@@ -8,12 +8,13 @@
 // Out[r, n] = scale * sum_k Band[r, k] * B[n, k]
 //
 // The band operand is stored in 128-row blocks, each with its own K window
-// [kb, kb + 64*nch) (kb a multiple of 64, zero filled outside the rows'
-// bands): rows r of block b hold Band[r, kb + x] at local column x.  B is
-// N rows of K (K contiguous, "K-major"): V^T for F.V, (2 F.V)^T for F^T.(.).
-// One CTA computes a 128 x BN tile: warp 0 lane 0 streams 64-wide K chunks
-// of A hi/lo and B hi/lo through a ring of shared-memory stages with TMA
-// (128-byte swizzle), warp 1 lane 0 issues the MMAs (M=128, N=BN, K=16,
+// [kb, kb + kTcK*nch) (kb a multiple of kTcK = 32, zero filled outside the
+// rows' bands): rows r of block b hold Band[r, kb + x] at local column x.  B
+// is N rows of K (K contiguous, "K-major"): V^T for F.V, (2 F.V)^T for
+// F^T.(.).  One CTA computes a 128 x BN tile: warp 0 lane 0 streams 32-wide
+// K chunks of A hi/lo and B hi/lo through a ring of up to 6 shared-memory
+// stages with TMA (64-byte rows, 64-byte swizzle: a BN = 256 stage is 48 KB,
+// so 4 stages fit beside the epilogue), warp 1 lane 0 issues the MMAs (M=128, N=BN, K=16,
 // bf16 in, FP32 accumulator in tensor memory), all four warps then read the
 // accumulator back (tcgen05.ld, one row per thread) and store it.
 //
@@ -34,8 +35,10 @@ namespace pqdts {
 
 constexpr int kTcThreads = 128;
 constexpr int kTcRows = 128;           // rows of a band block = MMA M
-constexpr int kTcK = 64;               // K per stage: one 128-byte swizzled row of bf16
-constexpr int kTcMaxStages = 4;
+constexpr int kTcK = 32;               // K per stage: one 64-byte swizzled row of bf16
+constexpr uint32_t kTcRowBytes = kTcK * 2;  // bytes of one operand row in a stage
+constexpr int kTcMaxStages = 6;
+static_assert(kTcRowBytes == 32 || kTcRowBytes == 64 || kTcRowBytes == 128, "swizzle width");
 constexpr uint64_t kTcWaitNs = 2000000000ull;  // 2 s per wait (default)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -136,15 +139,18 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
 }
 
 // Shared-memory matrix descriptor of a K-major operand tile written by TMA
-// with the 128-byte swizzle: rows of 128 bytes, 8-row groups 1024 bytes
-// apart (stride byte offset), tile base 1024-byte aligned; advancing the
-// start address by 32 bytes selects the next K=16 slice of the swizzled row.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
-  return (uint64_t)((saddr & 0x3FFFFu) >> 4)  // start address
-         | ((uint64_t)1 << 16)                // leading byte offset (unused for swizzled K-major)
-         | ((uint64_t)(1024 >> 4) << 32)      // stride byte offset
-         | ((uint64_t)1 << 46)                // descriptor version
-         | ((uint64_t)2 << 61);               // 128-byte swizzle
+// with the swizzle of its row width (kTcRowBytes = 128, 64 or 32 bytes):
+// 8-row groups 8 * kTcRowBytes apart (stride byte offset), tile base aligned
+// to 1024 bytes; advancing the start address by 32 bytes selects the next
+// K=16 slice of the swizzled row.  Layout field (bits 61-63): 2 = 128-byte,
+// 4 = 64-byte, 6 = 32-byte swizzle.
+__device__ __forceinline__ uint64_t swz_desc(uint32_t saddr) {
+  constexpr uint64_t layout = kTcRowBytes == 128 ? 2 : kTcRowBytes == 64 ? 4 : 6;
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4)           // start address
+         | ((uint64_t)1 << 16)                         // leading byte offset (unused for swizzled K-major)
+         | ((uint64_t)((8 * kTcRowBytes) >> 4) << 32)  // stride byte offset
+         | ((uint64_t)1 << 46)                         // descriptor version
+         | (layout << 61);                             // swizzle mode
 }
 
 // Instruction descriptor, kind::f16: FP32 accumulator, bf16 A and B, both
@@ -193,7 +199,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   // stage ring, 1024-byte aligned (swizzle atoms)
   const uint32_t raw = smem_u32(tc_smem_raw);
   uint8_t* base = tc_smem_raw + ((1024u - (raw & 1023u)) & 1023u);
-  const uint32_t a_bytes = kTcRows * 128u, b_bytes = (uint32_t)BN * 128u;
+  const uint32_t a_bytes = kTcRows * kTcRowBytes, b_bytes = (uint32_t)BN * kTcRowBytes;
   const uint32_t stage_bytes = 2u * a_bytes + 2u * b_bytes;
 
   if (threadIdx.x == 0) {
@@ -260,9 +266,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
       for (int k = 0; k < kTcK / 16; ++k) {
         const uint32_t o = 32u * k;
-        tc_mma(tmem, sw128_desc(a_lo + o), sw128_desc(b_hi + o), idesc, (it > 0 || k > 0) ? 1u : 0u);
-        tc_mma(tmem, sw128_desc(a_hi + o), sw128_desc(b_lo + o), idesc, 1u);
-        tc_mma(tmem, sw128_desc(a_hi + o), sw128_desc(b_hi + o), idesc, 1u);
+        tc_mma(tmem, swz_desc(a_lo + o), swz_desc(b_hi + o), idesc, (it > 0 || k > 0) ? 1u : 0u);
+        tc_mma(tmem, swz_desc(a_hi + o), swz_desc(b_lo + o), idesc, 1u);
+        tc_mma(tmem, swz_desc(a_hi + o), swz_desc(b_hi + o), idesc, 1u);
       }
       tc_commit(&bar_empty[st]);  // the stage is free once these MMAs are done
     }
@@ -360,8 +366,10 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 }
 
 // Persistent form of k_tc_band (same operands, modes and results): one CTA
-// per SM walks the output tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...
-// (N tiles fastest, then row blocks, then K splits).  Six warps: warp 0
+// per SM walks its list of output tiles sched_tile[sched_off[b] ..
+// sched_off[b+1]) (tile t: N tile t % ntn, then row block, then K split;
+// the host balances the lists by each tile's K chunks, longest first), or
+// with sched_off = null t = blockIdx.x, blockIdx.x + gridDim.x, ...  Six warps: warp 0
 // lane 0 issues the TMA loads, warp 1 lane 0 the MMAs (warp 1 owns the
 // tensor memory), warps 2-5 run the epilogue.  Two FP32 accumulators in
 // tensor memory let the epilogue of tile j overlap the MMAs of tile j+1,
@@ -374,7 +382,8 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
                 const int32_t* __restrict__ blk_kb, const int32_t* __restrict__ blk_nch, int R, int N, int BN,
                 int stages, int splits, int blocks, int mode, float scale, float* __restrict__ out,
                 int64_t out_stride, __nv_bfloat16* __restrict__ oh, __nv_bfloat16* __restrict__ ol, int64_t ld,
-                const double* __restrict__ pred, double* __restrict__ err, uint64_t wait_ns, int probe) {
+                const double* __restrict__ pred, double* __restrict__ err, uint64_t wait_ns, int probe,
+                const int32_t* __restrict__ sched_off, const int32_t* __restrict__ sched_tile) {
   if (pred != nullptr && pred[6] != 0.0) return;  // CG already converged
   extern __shared__ uint8_t tc_smem_raw[];
   __shared__ uint64_t bar_full[kTcMaxStages], bar_empty[kTcMaxStages], bar_tfull[2], bar_tempty[2], bar_fin,
@@ -389,7 +398,7 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
   const int T = ntn * blocks * splits;
   const uint32_t raw = smem_u32(tc_smem_raw);
   uint8_t* base = tc_smem_raw + ((1024u - (raw & 1023u)) & 1023u);
-  const uint32_t a_bytes = kTcRows * 128u, b_bytes = (uint32_t)BN * 128u;
+  const uint32_t a_bytes = kTcRows * kTcRowBytes, b_bytes = (uint32_t)BN * kTcRowBytes;
   const uint32_t stage_bytes = 2u * a_bytes + 2u * b_bytes;
   const uint32_t ncols = tc_tmem_cols(BN);  // per accumulator
 
@@ -423,6 +432,11 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
   tc_fence_after();
   const uint32_t tmem = s_tmem;
 
+  // this CTA's tiles: entries [j_begin, j_end) of its list (or the
+  // round-robin sequence blockIdx.x + j * gridDim.x)
+  const int j_begin = sched_off ? sched_off[blockIdx.x] : 0;
+  const int j_end = sched_off ? sched_off[blockIdx.x + 1] : (T - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+  auto tile_of = [&](int j) { return sched_off ? sched_tile[j] : (int)blockIdx.x + j * (int)gridDim.x; };
   // tile t -> N tile, row block, K chunk range [c0, c1), block K start kb
   auto tile = [&](int t, int& nt, int& blk, int& c0, int& c1, int& kb) {
     nt = t % ntn;
@@ -443,9 +457,9 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
     if (lane == 0) {
       int it = 0;
       if (probe && !mbar_wait(&bar_probe, 0, wait_ns)) s_abort = 1;  // nothing arrives: runs out
-      for (int t = blockIdx.x; t < T && !s_abort; t += gridDim.x) {
+      for (int j = j_begin; j < j_end && !s_abort; ++j) {
         int nt, blk, c0, c1, kb;
-        tile(t, nt, blk, c0, c1, kb);
+        tile(tile_of(j), nt, blk, c0, c1, kb);
         for (int ch = c0; ch < c1 && !s_abort; ++ch, ++it) {
           const int st = it % stages;
           const uint32_t ph = (uint32_t)(it / stages) & 1u;
@@ -468,13 +482,13 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       const uint32_t idesc = tc_idesc_bf16(kTcRows, BN);
-      int it = 0, j = 0;
-      for (int t = blockIdx.x; t < T && !s_abort; t += gridDim.x, ++j) {
+      int it = 0;
+      for (int j = j_begin; j < j_end && !s_abort; ++j) {
         int nt, blk, c0, c1, kb;
-        tile(t, nt, blk, c0, c1, kb);
-        const int buf = j & 1;
+        tile(tile_of(j), nt, blk, c0, c1, kb);
+        const int jj = j - j_begin, buf = jj & 1;
         const uint32_t acc = tmem + (uint32_t)buf * ncols;
-        if (!mbar_wait(&bar_tempty[buf], ((uint32_t)(j >> 1) & 1u) ^ 1u, wait_ns)) {  // accumulator free
+        if (!mbar_wait(&bar_tempty[buf], ((uint32_t)(jj >> 1) & 1u) ^ 1u, wait_ns)) {  // accumulator free
           s_abort = 1;
           break;
         }
@@ -493,9 +507,9 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
 #pragma unroll
           for (int k = 0; k < kTcK / 16; ++k) {
             const uint32_t o = 32u * k;
-            tc_mma(acc, sw128_desc(a_lo + o), sw128_desc(b_hi + o), idesc, (ch > c0 || k > 0) ? 1u : 0u);
-            tc_mma(acc, sw128_desc(a_hi + o), sw128_desc(b_lo + o), idesc, 1u);
-            tc_mma(acc, sw128_desc(a_hi + o), sw128_desc(b_hi + o), idesc, 1u);
+            tc_mma(acc, swz_desc(a_lo + o), swz_desc(b_hi + o), idesc, (ch > c0 || k > 0) ? 1u : 0u);
+            tc_mma(acc, swz_desc(a_hi + o), swz_desc(b_lo + o), idesc, 1u);
+            tc_mma(acc, swz_desc(a_hi + o), swz_desc(b_hi + o), idesc, 1u);
           }
           tc_commit(&bar_empty[st]);
         }
@@ -506,12 +520,12 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
   } else {
     // epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. + 31 = tile rows
     const int q = warp & 3, ew = warp - 2;
-    int j = 0;
-    for (int t = blockIdx.x; t < T; t += gridDim.x, ++j) {
+    for (int j = j_begin; j < j_end; ++j) {
+      const int t = tile_of(j);
       int nt, blk, c0, c1, kb;
       tile(t, nt, blk, c0, c1, kb);
-      const int nk = c1 - c0, buf = j & 1;
-      const bool ok = mbar_wait(&bar_tfull[buf], (uint32_t)(j >> 1) & 1u, wait_ns);
+      const int jj = j - j_begin, nk = c1 - c0, buf = jj & 1;
+      const bool ok = mbar_wait(&bar_tfull[buf], (uint32_t)(jj >> 1) & 1u, wait_ns);
       tc_fence_after();
       const bool store = __all_sync(0xffffffffu, ok && !s_abort);
       if (!store) {
@@ -631,6 +645,113 @@ __global__ void k_split_t(const float* __restrict__ V, int M, int N, int64_t ld,
       lo[(int64_t)n * ld + i] = __float2bfloat16_rn(x - __bfloat162float(h));
     }
   }
+}
+
+// Tensor-core mixed CG, one launch before the Hessian product: the p update
+// p = beta p + z (2075; skipped when do_update = 0, the first iteration),
+// then V = p, or in the reduced space BF's lift (260-267) V = p with entry
+// (i, maxr[i]) = -rs[i], rs[i] = sum(p(i,:)) - p(i,maxr[i]) (written to rs),
+// and V's transposed split hi[n * ld + i], lo[n * ld + i] (the F.V
+// product's K-major operand).  One block of 32 x Y threads owns 32 whole
+// rows (thread (x, y) always handles column x of rows y, y + Y, ...): in the
+// reduced space it first updates them and forms their sums (a warp tree per
+// row), then transposes the lifted rows tile by tile; in the full space it
+// updates and transposes in one pass.  Replaces k_cg_pupdate / k_cg_lift32
+// + k_split_t.
+template <int Y>
+__device__ __forceinline__ void cg_lift_split_body(int bx, const double* __restrict__ sc, int do_update, int M, int N,
+                                                   float* __restrict__ p, const float* __restrict__ z,
+                                                   const int32_t* __restrict__ maxr, float* __restrict__ rs,
+                                                   int64_t ld, __nv_bfloat16* __restrict__ hi,
+                                                   __nv_bfloat16* __restrict__ lo) {
+  static_assert(32 % Y == 0, "rows per thread");
+  constexpr int Q = 32 / Y;
+  __shared__ float t[32][33];
+  __shared__ float s_rest[32];
+  __shared__ int s_m[32];
+  const int tx = threadIdx.x, ty = threadIdx.y;  // blockDim = (32, Y)
+  const int i0 = bx * 32;
+  const float beta = do_update ? (float)sc[SC_V2] : 0.f;
+  const bool reduced = maxr != nullptr;
+  if (reduced) {
+    // pass 1: update the block's rows, sum them
+    float sum[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) sum[q] = 0.f;
+    for (int n0 = 0; n0 < N; n0 += 32) {
+      const int n = n0 + tx;
+#pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        const int i = i0 + ty + Y * q;
+        if (i < M && n < N) {
+          const int64_t k = (int64_t)i * N + n;
+          float pv = p[k];
+          if (do_update) {
+            pv = fmaf(beta, pv, z[k]);
+            p[k] = pv;
+          }
+          sum[q] += pv;
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) sum[q] += __shfl_xor_sync(0xffffffffu, sum[q], o);
+    __syncthreads();  // the updated rows are visible to the whole block
+    if (tx == 0) {
+#pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        const int r = ty + Y * q, i = i0 + r;
+        if (i < M) {
+          const int m = min(max(maxr[i], 0), N - 1);
+          const float rest = sum[q] - p[(int64_t)i * N + m];
+          s_rest[r] = rest;
+          s_m[r] = m;
+          rs[i] = rest;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // transpose tile by tile (pass 2 in the reduced space)
+  for (int n0 = 0; n0 < N; n0 += 32) {
+    for (int rr = ty; rr < 32; rr += Y) {
+      const int i = i0 + rr, n = n0 + tx;
+      float v = 0.f;
+      if (i < M && n < N) {
+        const int64_t k = (int64_t)i * N + n;
+        v = p[k];
+        if (!reduced && do_update) {
+          v = fmaf(beta, v, z[k]);
+          p[k] = v;
+        }
+        if (reduced && n == s_m[rr]) v = -s_rest[rr];
+      }
+      t[rr][tx] = v;
+    }
+    __syncthreads();
+    for (int rr = ty; rr < 32; rr += Y) {
+      const int n = n0 + rr, i = i0 + tx;
+      if (n < N && i < M) {
+        const float x = t[tx][rr];
+        const __nv_bfloat16 h = __float2bfloat16_rn(x);
+        hi[(int64_t)n * ld + i] = h;
+        lo[(int64_t)n * ld + i] = __float2bfloat16_rn(x - __bfloat162float(h));
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <int Y>
+__global__ void __launch_bounds__(32 * Y) k_cg_lift_split(const double* __restrict__ sc, int do_update, int M, int N,
+                                                          float* __restrict__ p, const float* __restrict__ z,
+                                                          const int32_t* __restrict__ maxr, float* __restrict__ rs,
+                                                          int64_t ld, __nv_bfloat16* __restrict__ hi,
+                                                          __nv_bfloat16* __restrict__ lo) {
+  if (sc != nullptr && sc[SC_DONE] != 0.0) return;
+  cg_lift_split_body<Y>(blockIdx.x, sc, do_update, M, N, p, z, maxr, rs, ld, hi, lo);
 }
 
 }  // namespace pqdts

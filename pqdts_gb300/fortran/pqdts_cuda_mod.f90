@@ -260,6 +260,17 @@ module pqdts_cuda_mod
       type(c_ptr), value :: target_L
     end function
 
+    ! the grouping pqdts_cuda_solve_batch uses (lockstep groups sharing F); host only
+    integer(c_int32_t) function pqdts_cuda_batch_groups(n_inst, M, N, D, band_lo, band_hi, band_vals, &
+                                                        band_row_offset, band_val_offset, group_of) &
+        bind(C, name="pqdts_cuda_batch_groups")
+      import :: c_int32_t, c_int64_t, c_double
+      integer(c_int32_t), value :: n_inst
+      integer(c_int64_t) :: M(*), N(*), D(*), band_lo(*), band_hi(*), band_row_offset(*), band_val_offset(*)
+      real(c_double) :: band_vals(*)
+      integer(c_int32_t) :: group_of(*)
+    end function
+
     ! smoothing of a restart state, pqdts.f90:1877-1902 (host memory, no context)
     integer(c_int32_t) function pqdts_cuda_smooth(M, N, smo_fact, X) bind(C, name="pqdts_cuda_smooth")
       import :: c_int32_t, c_int64_t, c_double

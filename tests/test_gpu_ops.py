@@ -172,6 +172,36 @@ def test_internal_F(built):
         assert np.array_equal(s.maxr(), o.maxr())
 
 
+@pytest.mark.parametrize("D", [21, 61])
+def test_internal_F_on_device(built, D):
+    """Internal F computed on the device (option internal_f = 1; the default
+    for mixed problems): the same windows as the host's (the oracle's), and
+    values within 1e-12 relative (CUDA's lgamma / exp / log against the
+    host's libm), seen through F.X at a positive X."""
+    import pqdts_gb300 as pq
+    from oracle.oracle import Oracle
+
+    M, N = (D - 1) ** 2, 8
+    o = Oracle(M, N, D, 1e-4, None, None)
+    olo, ohi, _, oval = o.bands()
+    X = _random_x(type("I", (), {"M": M, "N": N})(), 12)
+    Oo = o.redO(X)
+    for prec, opt in ((pq.FP64, 1), (pq.MIXED, -1)):
+        with pq.Solver(0) as s:
+            s.set_option("internal_f", opt)
+            s.set_problem_coo(M, N, D, None, None, 1e-4, prec)
+            lo, hi, nnz = s.bands()
+            assert np.array_equal(lo, olo) and np.array_equal(hi, ohi) and nnz == oval.size
+            s.set_x(X)
+            Og = s.redO()
+            assert np.max(np.abs(Og - Oo) / np.maximum(np.abs(Oo), 1e-300)) <= 1e-12
+            if prec == pq.MIXED:
+                st = s.solve(mode=2, maxiter=30, eps=1e-6)
+                Xs = s.get_x()
+                assert np.isfinite(st["L"]) and Xs.min() >= 0.0
+                assert np.max(np.abs(Xs.sum(axis=1) - 1.0)) <= 1e-12
+
+
 def test_errors_are_codes(built):
     import pqdts_gb300 as pq
 

@@ -121,6 +121,35 @@ def test_batch_matches_single(built):
         _feasible(X, exact=True)
 
 
+def test_batch_groups_lockstep(built, monkeypatch):
+    """Mixed-precision instances that share F (resampled P, a gamma sweep)
+    are solved in lockstep groups with a joint CG: every instance reaches its
+    FP64 objective (conv < 1e-9 pins it) to 1e-8 relative, Pi >= 0 exactly,
+    as the same batch does with the grouping off."""
+    import pqdts_gb300 as pq
+    from pqdts_gb300 import synth
+
+    insts = synth.make_batch(n_base=2, n_resample=3, shots=10**6, seed=4, m_range=(60, 150), n_range=(33, 60))
+    groups = pq.batch_groups(insts)
+    assert list(groups) == [0, 0, 0, 1, 1, 1]
+    _, st64 = pq.solve_batch(insts, precision=pq.FP64, maxiter=2000, eps=1e-9)
+    L64 = np.array([x["L"] for x in st64])
+    for flag in ("1", "0"):
+        monkeypatch.setenv("PQDTS_BATCH_GROUPS", flag)
+        Xm, sm = pq.solve_batch(insts, precision=pq.MIXED, maxiter=2000, eps=1e-9)
+        for X, st, l64 in zip(Xm, sm, L64):
+            assert abs(st["L"] - l64) <= MIXED_OBJ_REL * abs(l64), (flag, st, l64)
+            _feasible(X, exact=True)
+    # the benchmark's stopping rule: each member stops at its own target
+    monkeypatch.setenv("PQDTS_BATCH_GROUPS", "1")
+    _, st6 = pq.solve_batch(insts, precision=pq.FP64, maxiter=200, eps=1e-6)
+    tg = np.array([x["L"] for x in st6]) * (1.0 + 1e-8)
+    Xm, sm = pq.solve_batch(insts, precision=pq.MIXED, maxiter=400, eps=1e-300, targets=tg)
+    for X, st, t in zip(Xm, sm, tg):
+        assert st["L"] <= t and st["cg"] > 0
+        _feasible(X, exact=True)
+
+
 @pytest.mark.parametrize("which", ["cfg1", "small"])
 def test_fp64_tight_tolerance_matches_oracle(built, request, which):
     """At conv < 1e-9 the objective is pinned; the tolerance form of the bar."""

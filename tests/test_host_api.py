@@ -85,3 +85,23 @@ def test_run_pqdts_dry_run_needs_no_gpu():
     assert pq.run_pqdts(3, 4, 6, P, F=sps.csr_matrix(np.ones((6, 4))), dry=True) is None
     with pytest.raises(ValueError):
         pq.run_pqdts(3, 4, 6, P, F=sps.csr_matrix(np.ones((5, 4))), dry=True)
+
+
+def test_batch_groups_host_only(built):
+    """The batch's lockstep grouping is a host computation: instances with
+    identical F (and 32 <= N <= 1024) share a group, others are alone."""
+    import dataclasses
+
+    import pqdts_gb300 as pq
+    from pqdts_gb300 import synth
+
+    insts = synth.make_batch(n_base=2, n_resample=3, shots=10**6, seed=4, m_range=(60, 150), n_range=(33, 60))
+    assert list(pq.batch_groups(insts)) == [0, 0, 0, 1, 1, 1]
+    # one changed F value splits that instance off
+    v = insts[1].band_val.copy()
+    v[5] *= 1.0 + 1e-15
+    changed = insts[:3] + [dataclasses.replace(insts[1], band_val=v)]
+    assert list(pq.batch_groups(changed)) == [0, 0, 0, -1]
+    # N below a warp: solved alone
+    small = synth.make_batch(n_base=1, n_resample=3, shots=10**6, seed=4, m_range=(40, 90), n_range=(5, 12))
+    assert list(pq.batch_groups(small)) == [-1, -1, -1]
