@@ -352,6 +352,7 @@ def north_star_config3(local, dev):
                        "from Pi=1/N", "nnz_F": inst.nnz, "generation_s": time.perf_counter() - t0}
     clk = Clocks(local).start()
     with pq.Solver(local) as s:
+        s.set_option("timers", 0)
         s.set_instance(inst, pq.FP64)
         timed_solve(s, dev, EPS, maxiter=2)  # warm-up: captures both stages' CG graphs
         t64, st64 = timed_solve(s, dev, EPS)
@@ -364,10 +365,12 @@ def north_star_config3(local, dev):
         with pq.Solver(local) as s:
             s.set_option("tensor_cores", tc)
             s.set_instance(inst, pq.MIXED)
-            timed_solve(s, dev, 1e-300, L64 * (1.0 + OBJ_REL))  # warm-up
             b0 = s.timer("BF")
-            tm, sm = timed_solve(s, dev, 1e-300, L64 * (1.0 + OBJ_REL))
+            timed_solve(s, dev, 1e-300, L64 * (1.0 + OBJ_REL))  # warm-up, region timers on
             b1 = s.timer("BF")
+            s.set_option("timers", 0)
+            timed_solve(s, dev, 1e-300, L64 * (1.0 + OBJ_REL))  # warm-up without them
+            tm, sm = timed_solve(s, dev, 1e-300, L64 * (1.0 + OBJ_REL))
             Xm = s.get_x()
             bft, bfn = b1[0] - b0[0], b1[1] - b0[1]
             pair = {"calls": bfn, "us_per_call": bft / bfn * 1e6 if bfn else None,
@@ -467,8 +470,14 @@ def run_ours(args):
         s = pq.Solver(local)
         s.set_instance(inst, pq.MIXED)
         eps_run, tgt = 1e-300, target
-    timed_solves(s, args.warmup, eps_run, tgt)
+    # the region timers (CUDA events, ~4 us per span inside a captured CG
+    # graph) are read from one solve; the warm-up and timed solves run
+    # without them
     bf0 = s.timer("BF")
+    _, st_t = timed_solves(s, 1, eps_run, tgt)
+    bf1 = s.timer("BF")
+    s.set_option("timers", 0)
+    timed_solves(s, args.warmup, eps_run, tgt)
     launches0 = s.kernel_launches()
     clocks = Clocks(local)
     dist_barrier(dist)
@@ -481,7 +490,6 @@ def run_ours(args):
     t_wall = time.perf_counter() - t_wall
     clk = clocks.stop()
     launches = s.kernel_launches() - launches0
-    bf1 = s.timer("BF")
     step_s = dist_max(dist, statistics.mean(times), dev)
     rel_err = abs(stats[-1]["L"] - L64) / abs(L64)
     if prec == pq.FP64:
@@ -494,7 +502,7 @@ def run_ours(args):
     # roofline of the dominant kernels: the banded products of the CG's
     # Hessian product (k_fwd + k_trans), FP64- (or FP32-) ALU bound.
     nnz, N, M, D = inst.nnz, inst.N, inst.M, inst.D
-    cg = sum(x["cg"] for x in stats)
+    cg = st_t[0]["cg"]  # the CG iterations of the solve whose regions were timed
     bf_time = bf1[0] - bf0[0]
     flops_pair = 2 * 2.0 * nnz * N
     achieved_tf = flops_pair * cg / bf_time / 1e12 if bf_time > 0 else None
@@ -510,6 +518,7 @@ def run_ours(args):
     traffic = profile_traffic("spmm_fp64_config2.txt" if prec == pq.FP64 else "spmm_fp32_config2.txt")
     roofline = {
         "kernel": "k_fwd + k_trans (Hessian product: O = F.V, F^T.(2O) + stencil)",
+        "timed": "GPU events around the CG's Hessian products in one solve of the workload (region timers on)",
         "bound": "fp64" if prec == pq.FP64 else "fp32",
         "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
         "frac": (achieved_tf / peak_tf) if (achieved_tf and peak_tf) else None,
@@ -531,6 +540,7 @@ def run_ours(args):
     for _ in range(max(1, args.steps)):
         torch.cuda.synchronize()
         with pq.Solver(local) as se:
+            se.set_option("timers", 0)
             se.set_objective_target(tgt)
             a0 = se.transfer_bytes()
             t0 = time.perf_counter()
@@ -551,14 +561,16 @@ def run_ours(args):
             with pq.Solver(local) as sm:
                 sm.set_option("tensor_cores", tc)
                 sm.set_instance(inst, pq.MIXED)
-                timed_solves(sm, args.warmup, 1e-300, target)
                 b0, l0, g0 = sm.timer("BF"), sm.timer("L"), sm.timer("dL")
+                _, mst = timed_solves(sm, 1, 1e-300, target)  # the region timers' solve
+                b1, l1, g1 = sm.timer("BF"), sm.timer("L"), sm.timer("dL")
+                sm.set_option("timers", 0)
+                timed_solves(sm, args.warmup, 1e-300, target)
                 ck = Clocks(local).start()
                 mt, ms = timed_solves(sm, args.steps, 1e-300, target)
                 mclk = ck.stop()
-                b1, l1, g1 = sm.timer("BF"), sm.timer("L"), sm.timer("dL")
                 mval = statistics.mean(mt)
-                cgs = sum(x["cg"] for x in ms)
+                cgs = mst[0]["cg"]
                 bft = b1[0] - b0[0]
                 Xm = sm.get_x()
                 out = {"value": mval, "unit": "s", "speedup_vs_fp64": step_s / mval,
@@ -569,8 +581,9 @@ def run_ours(args):
                        "double_fp32_gradient_and_checks": bool(sm.get_option("sched.df_trans")),
                        # GPU time per solve in the objective (L: checks of the chosen
                        # steps) and gradient (dL) regions, double-FP32 products included
-                       "L_region_s_per_solve": (l1[0] - l0[0]) / len(mt),
-                       "dL_region_s_per_solve": (g1[0] - g0[0]) / len(mt),
+                       # (the region timers' solve)
+                       "L_region_s_per_solve": l1[0] - l0[0],
+                       "dL_region_s_per_solve": g1[0] - g0[0],
                        "max_abs_pi_vs_fp64": float(np.max(np.abs(Xm - X64))), "min_pi": float(Xm.min()),
                        "max_row_sum_err": float(np.max(np.abs(Xm.sum(axis=1) - 1.0))),
                        "hessian_product_pair": {"us_per_cg_iteration": bft / cgs * 1e6 if cgs else None,
@@ -645,7 +658,10 @@ def run_profile_case(case):
       fp64 / mixed: the Hessian product (3x BF resp. BF32), then 3x dL and
         3x L at a random feasible X -- real banded-product launches only
         (fp64: row-flattened products, no autotuning launches);
-      solve64 / solvemix: one full benchmark solve (the launch list)."""
+      solve64 / solvemix: one full benchmark solve (the launch list);
+      solvemix3: the mixed solve of M=10000 N=1000 D=20000 to its own
+        stopping rule conv < 1e-6 (no FP64 solve first: the launch list of
+        the mixed solver alone)."""
     import numpy as np
 
     import pqdts_gb300 as pq
@@ -666,6 +682,15 @@ def run_profile_case(case):
             for _ in range(3):
                 s.BF32(V)
             print(json.dumps({"profile_case": case, "launches": s.kernel_launches(), "nnz": inst.nnz}))
+        return 0
+    if case == "solvemix3":
+        inst = synth.make_config(3, seed=0)
+        with pq.Solver(0) as s:
+            s.set_option("timers", 0)
+            s.set_instance(inst, pq.MIXED)
+            st = s.solve(mode=2, maxiter=MAXITER, eps=EPS)
+            print(json.dumps({"profile_case": case, "stats": st, "launches": s.kernel_launches(),
+                              "schedule": s.schedule()}))
         return 0
     inst = synth.make_config(CONFIG, seed=0)
     prec = pq.MIXED if case in ("mixed", "solvemix") else pq.FP64
@@ -804,8 +829,8 @@ def main():
     ap.add_argument("--no-mixed", dest="with_mixed", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-sample-iters", type=int, default=3)
-    ap.add_argument("--profile-case", choices=["fp64", "mixed", "solve64", "solvemix", "tc3", "tcdense", "tc3p",
-                                               "tcdensep"], default=None,
+    ap.add_argument("--profile-case", choices=["fp64", "mixed", "solve64", "solvemix", "solvemix3", "tc3", "tcdense",
+                                               "tc3p", "tcdensep"], default=None,
                     help="launches of the workload for ncu (see run_profile_case)")
     ap.add_argument("--workload", choices=["batch", "config3", "dense", "config5"], default=None,
                     help="secondary measurement instead of the bench line")

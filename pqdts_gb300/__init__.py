@@ -289,7 +289,7 @@ class Solver:
     def schedule(self):
         """Launch schedule of the banded products in use (autotuned or heuristic)."""
         keys = ("fwd_tile", "trn_tile", "trn_splits", "trans_threads", "trans_cols", "tuned", "tc", "tc_bn",
-                "tc_splits", "tc_splits1", "tc_persistent", "df_fwd", "df_trans")
+                "tc_splits", "tc_splits1", "tc_persistent", "df_fwd", "df_trans", "tc_screen")
         return {k: self.get_option("sched." + k) for k in keys}
 
     def kernel_launches(self):

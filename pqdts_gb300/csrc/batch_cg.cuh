@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(32 * Y) k_cg_lift_split_b(const CGMember* __re
 
 // Hraw: the group's transposed product partials, (M, G*N) row-major per
 // split, member j's columns j*N .. j*N + N-1.
-__global__ void __launch_bounds__(1024) k_hvp_epi32_rows_b(const CGMember* __restrict__ mem,
+__global__ void __launch_bounds__(256) k_hvp_epi32_rows_b(const CGMember* __restrict__ mem,
                                                          const float* __restrict__ Hraw, int64_t hstride,
                                                          int64_t hplane, int M, int N, int RB, int parts) {
   const CGMember& m = mem[blockIdx.y];

@@ -292,7 +292,7 @@ struct TcOperand {
   std::vector<int32_t> h_nch;  // K chunks per row block (host copy: the tile costs)
   int blocks = 0, kmax = 0;
   CUtensorMap map_hi, map_lo;
-  std::map<std::pair<int, int>, std::unique_ptr<TcSched>> scheds;  // keyed by (BN, splits)
+  std::map<std::array<int, 3>, std::unique_ptr<TcSched>> scheds;  // keyed by (BN, splits, N)
 };
 
 // CG work vectors of one precision.
@@ -400,6 +400,15 @@ struct pqdts_ctx {
   pqdts::DBuf<__nv_bfloat16> vt_hi, vt_lo, yt_hi, yt_lo;
   pqdts::DBuf<float> ypart;  // FP32 partials of F.V when its K range is split
   CUtensorMap map_vt_hi, map_vt_lo, map_yt_hi, map_yt_lo;
+  // the line search's probes dX^T split (kBatchLS * N rows of tc_mp) for
+  // their F products on the tensor cores, and its maps (built for the tile
+  // width, buffer and stride recorded beside them)
+  pqdts::DBuf<__nv_bfloat16> ls_hi, ls_lo;
+  CUtensorMap map_ls_hi, map_ls_lo;
+  int ls_map_bn = 0;
+  const void* ls_map_ptr = nullptr;
+  int64_t ls_map_mp = 0, ls_map_rows = 0;
+  int tc_screen_option = -1;  // line-search screen on the tensor cores: -1 auto (with the CG's), 0 off
   pqdts::Schedule sched;
   bool own_stream = true;  // false: a member of a batched group, on the group's stream
   // group context of a batched lockstep solve: the members' CG table
@@ -1125,14 +1134,15 @@ static void setup_tc(Ctx& c) {
 // sorted by their K chunks, longest first, each given to the CTA with the
 // least work so far (+2 chunks of fixed cost per tile); built once per
 // problem and shape, outside any stream capture.
-static TcSched& tc_sched(Ctx& c, TcOperand& A, int bn, int splits) {
-  auto key = std::make_pair(bn, splits);
+static TcSched& tc_sched(Ctx& c, TcOperand& A, int bn, int splits, int N = -1) {
+  if (N < 0) N = (int)c.h.N;
+  const std::array<int, 3> key{bn, splits, N};
   auto it = A.scheds.find(key);
   if (it != A.scheds.end()) return *it->second;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   CK(cudaStreamIsCapturing(c.st, &cs));
   if (cs != cudaStreamCaptureStatusNone) throw Err(PQDTS_E_STATE, "internal: tensor-core tile lists built in a capture");
-  const int ntn = cdiv(c.h.N, bn);
+  const int ntn = cdiv(N, bn);
   const int64_t T = (int64_t)ntn * A.blocks * splits;
   const int grid = (int)std::min<int64_t>(T, c.num_sms);
   std::vector<std::pair<int, int32_t>> cost((size_t)T);
@@ -1168,15 +1178,16 @@ static TcSched& tc_sched(Ctx& c, TcOperand& A, int bn, int splits) {
 }
 
 // Out = scale * A . B^T on the tensor cores (A a TcOperand of R rows; B the
-// K-major split operand behind bhi / blo); mode 0: FP32 partials (splits of
-// the K range, out_stride apart), mode 1: transposed bf16 split into oh / ol.
+// K-major split operand behind bhi / blo, Nw rows: the problem's N unless
+// given); mode 0: FP32 partials (splits of the K range, out_stride apart),
+// mode 1: transposed bf16 split into oh / ol.
 static void tc_product(Ctx& c, TcOperand& A, const CUtensorMap& bhi, const CUtensorMap& blo, int R, int splits,
                        int mode, float scale, float* out, __nv_bfloat16* oh, __nv_bfloat16* ol, int64_t ld,
-                       const double* pred, int persistent) {
-  const int N = (int)c.h.N;
+                       const double* pred, int persistent, int Nw = -1) {
+  const int N = Nw > 0 ? Nw : (int)c.h.N;
   const size_t smem = (size_t)c.tc_stages * tc_stage_bytes(c.tc_bn) + 1024;
   if (persistent) {
-    TcSched& ts = tc_sched(c, A, c.tc_bn, splits);
+    TcSched& ts = tc_sched(c, A, c.tc_bn, splits, N);
     k_tc_band_p<<<ts.grid, kTcpThreads, smem, c.st>>>(A.map_hi, A.map_lo, bhi, blo, A.kb.p, A.nch.p, R, N, c.tc_bn,
                                                       c.tc_stages, splits, A.blocks, mode, scale, out, (int64_t)R * N,
                                                       oh, ol, ld, pred, c.sc.p + SC_TCERR, c.tc_wait_ns,
@@ -1226,6 +1237,41 @@ static void tc_hvp_products(Ctx& c, const float* src, const double* pred, bool p
              pred, c.sched.tc_persistent);
 }
 
+// The line-search probes' split operand and its maps (allocated on first
+// use, zero filled: rows beyond nb * N feed only columns that are never
+// stored; maps rebuilt when the tile width, buffer or stride changed).
+static void ensure_ls_operand(Ctx& c) {
+  const int64_t rows = (int64_t)kBatchLS * c.h.N;
+  const size_t need = (size_t)rows * (size_t)c.tc_mp;
+  if (c.ls_hi.p == nullptr || c.ls_hi.cap < need) {
+    c.ls_hi.alloc(need);
+    c.ls_lo.alloc(need);
+    CK(cudaMemsetAsync(c.ls_hi.p, 0, need * sizeof(__nv_bfloat16), c.st));
+    CK(cudaMemsetAsync(c.ls_lo.p, 0, need * sizeof(__nv_bfloat16), c.st));
+  }
+  if (c.ls_map_bn != c.tc_bn || c.ls_map_ptr != c.ls_hi.p || c.ls_map_mp != c.tc_mp || c.ls_map_rows != rows) {
+    make_map_bf16(&c.map_ls_hi, c.ls_hi.p, c.h.M, rows, (uint64_t)c.tc_mp * 2, kTcK, c.tc_bn);
+    make_map_bf16(&c.map_ls_lo, c.ls_lo.p, c.h.M, rows, (uint64_t)c.tc_mp * 2, kTcK, c.tc_bn);
+    c.ls_map_bn = c.tc_bn;
+    c.ls_map_ptr = c.ls_hi.p;
+    c.ls_map_mp = c.tc_mp;
+    c.ls_map_rows = rows;
+  }
+}
+
+// F.dX of nb line-search probes (Xc[0..nb) against X0) on the tensor cores:
+// one product over the probes' N' = nb * N columns into fdx32 (D x N'
+// row-major FP32; probe b's columns b * N ..).
+static void tc_probe_products(Ctx& c, const double* Xc, const double* X0, int nb) {
+  const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
+  ensure_ls_operand(c);
+  k_delta_split_t<<<dim3(cdiv(M, 32), cdiv(N, 32), nb), dim3(32, 8), 0, c.st>>>(Xc, X0, M, N, c.tc_mp, c.ls_hi.p,
+                                                                               c.ls_lo.p);
+  post_launch(c);
+  tc_product(c, c.tcF, c.map_ls_hi, c.map_ls_lo, D, 1, 0, 1.0f, c.fdx32.p, nullptr, nullptr, 0, nullptr,
+             c.sched.tc_persistent, nb * N);
+}
+
 // Out (R x N) = scale * Band (R rows) . In with tile code `tile` (0 = 64x64,
 // 1 = 64x32, 2 = 32x32 rows x columns); grid.z = nz stacked products
 // (in_stride / out_stride apart) or, with splits > 1, the K segments of one
@@ -1269,21 +1315,28 @@ static int heuristic_tile(int R, int N, int nz = 1) {
   return 2;
 }
 
-// The FP32 Hessian row epilogue over hpart32's `parts` partials (row-
-// flattened where it applies); returns the number of p.Hp partials written,
-// or 0 when the row-flattened form has already summed them into *vsum (its
+// Rows per block of the multi-row Hessian epilogue: about four blocks per
+// SM over the M rows, at most kEpiMaxRows.
+static int epi_rows(const Ctx& c, int64_t M) {
+  const int64_t want = M / std::max<int64_t>(1, 4 * (c.num_sms > 0 ? c.num_sms : 152));
+  return (int)std::max<int64_t>(1, std::min<int64_t>(want, kEpiMaxRows));
+}
+constexpr int kEpiThreads = 256;
+
+// The FP32 Hessian row epilogue over hpart32's `parts` partials (several
+// rows per block, streaming); returns the number of p.Hp partials written,
+// or 0 when the multi-row form has already summed them into *vsum (its
 // last block, vsum != null).
 static int hvp_epilogue(Ctx& c, const float* p, const float* rs, const int8_t* ik, float* Hp, double* dpart,
                         const double* pred, int parts, double* vsum = nullptr) {
   const int M = (int)c.h.M, N = (int)c.h.N;
-  const int RB = rows_per_block(N);
-  if (RB > 0 && c.rows_option != 0) {
-    const int threads = cdiv((int64_t)RB * N, 32) * 32;
+  const int RB = epi_rows(c, M);
+  if (c.rows_option != 0) {
     const bool fused = vsum != nullptr && dpart != nullptr;
-    k_hvp_epi32_rows<<<cdiv(M, RB), threads, 0, c.st>>>(c.hpart32.p, p, rs, c.maxr.p, rs ? 1 : 0,
-                                                         (float)(2.0 * c.h.gam), ik, M, N, RB, Hp, dpart, pred,
-                                                         parts, fused ? vsum : nullptr,
-                                                         fused ? c.counters.p + 4 : nullptr);
+    k_hvp_epi32_rows<<<cdiv(M, RB), kEpiThreads, 0, c.st>>>(c.hpart32.p, p, rs, c.maxr.p, rs ? 1 : 0,
+                                                            (float)(2.0 * c.h.gam), ik, M, N, RB, Hp, dpart, pred,
+                                                            parts, fused ? vsum : nullptr,
+                                                            fused ? c.counters.p + 4 : nullptr);
     post_launch(c);
     return fused ? 0 : cdiv(M, RB);
   }
@@ -1728,6 +1781,7 @@ static void line_search_mixed(Ctx& c, bool stage2, double& alpha, double& dlalph
   k_half_to32<<<elem_grid(DN), 256, 0, c.st>>>(c.R.p, DN, 0.5f, c.r0_32.p);
   post_launch(c);
   const int g = elem_grid(MN), g2 = elem_grid(DN);
+  const bool tc_screen = c.sched.tc && c.tc_ready && c.tc_screen_option != 0;
   // objective changes L(X_a) - L(X0) of nb projected probes -> dL[], xmin[]
   auto screen = [&](const double* qa, int nb, double* dL, double* xmin) {
     CK(cudaMemcpyAsync(c.alphas.p, qa, nb * sizeof(double), cudaMemcpyHostToDevice, c.st));
@@ -1746,11 +1800,18 @@ static void line_search_mixed(Ctx& c, bool stage2, double& alpha, double& dlalph
       post_launch(c);
       reduce_to(c, c.part2.p, gg, c.lsout.p + kBatchLS, nb);
     }
-    k_delta32<<<dim3(g, nb), 256, 0, c.st>>>(c.Xc.p, c.x0c.p, MN, c.d32.p);
-    post_launch(c);
-    launch_band_gemm32(c, heuristic_tile(D, N, nb), c.flo.p, c.fw.p, c.foff.p, c.fval32.p, c.d32.p, D, N, 1.0f,
-                       c.fdx32.p, nullptr, nb, MN, DN);
-    k_dres_part<<<dim3(g2, nb), 256, 0, c.st>>>(c.fdx32.p, c.r0_32.p, c.flo.p, D, N, c.part.p);
+    if (tc_screen) {
+      // one tensor-core product over the probes' columns (split-BF16x3,
+      // FP32 accumulation: F.dX to ~2^-16 of itself)
+      tc_probe_products(c, c.Xc.p, c.x0c.p, nb);
+      k_dres_part<<<dim3(g2, nb), 256, 0, c.st>>>(c.fdx32.p, c.r0_32.p, c.flo.p, D, N, (int64_t)nb * N, N, c.part.p);
+    } else {
+      k_delta32<<<dim3(g, nb), 256, 0, c.st>>>(c.Xc.p, c.x0c.p, MN, c.d32.p);
+      post_launch(c);
+      launch_band_gemm32(c, heuristic_tile(D, N, nb), c.flo.p, c.fw.p, c.foff.p, c.fval32.p, c.d32.p, D, N, 1.0f,
+                         c.fdx32.p, nullptr, nb, MN, DN);
+      k_dres_part<<<dim3(g2, nb), 256, 0, c.st>>>(c.fdx32.p, c.r0_32.p, c.flo.p, D, N, N, DN, c.part.p);
+    }
     post_launch(c);
     reduce_to(c, c.part.p, g2, c.lsout.p + 3 * kBatchLS, nb);
     CK(cudaMemcpyAsync(c.pin, c.lsout.p, 4 * kBatchLS * sizeof(double), cudaMemcpyDeviceToHost, c.st));
@@ -2257,8 +2318,7 @@ static void group_cg32(Ctx& g, std::vector<MemberRun>& ms, const std::vector<int
   CK(cudaMemsetAsync(g.sc.p + SC_DONE, 0, sizeof(double), g.st));
   const int active = (int)in_cg.size();
   const CGGroup grp{g.counters.p + 6, g.sc.p, active};
-  const int RB = rows_per_block(N);
-  const int rthreads = cdiv((int64_t)RB * N, 32) * 32;
+  const int RB = epi_rows(g, M);
   const int gs = std::min(elem_grid((int64_t)M * N), cdiv(M, 8));
   auto iteration = [&](bool first) {
     k_cg_lift_split_b<32><<<dim3(cdiv(M, 32), G), dim3(32, 32), 0, g.st>>>(g.memtab.p, first ? 0 : 1, M, N, g.tc_mp,
@@ -2267,8 +2327,9 @@ static void group_cg32(Ctx& g, std::vector<MemberRun>& ms, const std::vector<int
     tc_forward(g, g.sched.tc_splits1, g.sched.tc_persistent, g.sc.p);
     tc_product(g, g.tcFt, g.map_yt_hi, g.map_yt_lo, M, g.sched.tc_splits, 0, 1.0f, g.hpart32.p, nullptr, nullptr, 0,
                g.sc.p, g.sched.tc_persistent);
-    k_hvp_epi32_rows_b<<<dim3(cdiv(M, RB), G), rthreads, 0, g.st>>>(g.memtab.p, g.hpart32.p, Nw, (int64_t)M * Nw, M,
-                                                                     N, RB, g.sched.tc_splits);
+    k_hvp_epi32_rows_b<<<dim3(cdiv(M, RB), G), kEpiThreads, 0, g.st>>>(g.memtab.p, g.hpart32.p, Nw,
+                                                                        (int64_t)M * Nw, M, N, RB,
+                                                                        g.sched.tc_splits);
     post_launch(g);
     k_cg_step32_b<<<dim3(gs, G), 256, 0, g.st>>>(g.memtab.p, grp, M, N, kMaxCG);
     post_launch(g);
@@ -2281,12 +2342,11 @@ static void group_cg32(Ctx& g, std::vector<MemberRun>& ms, const std::vector<int
   }
 }
 
-// Whether a group of `members` instances of this shape can take the joint
-// CG: tensor-core products on the group context and the row-flattened
-// epilogue (32 <= N <= 1024).
+// Whether a group of instances of this shape can take the joint CG:
+// tensor-core products on the group context and the multi-row epilogue.
 static bool group_ready(const Ctx& g, int64_t N) {
-  return g.have_problem && g.precision == PQDTS_MIXED && g.sched.tc && g.tc_ready && rows_per_block((int)N) > 0 &&
-         g.rows_option != 0;
+  (void)N;
+  return g.have_problem && g.precision == PQDTS_MIXED && g.sched.tc && g.tc_ready && g.rows_option != 0;
 }
 
 static void group_solve(Ctx& g, std::vector<MemberRun>& ms) {
@@ -3208,6 +3268,9 @@ int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
     } else if (n == "tc_persistent") {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "tc_persistent must be -1, 0 or 1");
       c->tc_persistent_option = (int)value;
+    } else if (n == "tc_screen") {
+      if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "tc_screen must be -1, 0 or 1");
+      c->tc_screen_option = (int)value;
     } else if (n == "tensor_cores") {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "tensor_cores must be -1, 0 or 1");
       c->tc_option = (int)value;
@@ -3261,6 +3324,7 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     else if (n == "sched.trans_rows") *value = s.trans_rows;
     else if (n == "rows_kernels") *value = c->rows_option;
     else if (n == "tc_persistent") *value = c->tc_persistent_option;
+    else if (n == "tc_screen") *value = c->tc_screen_option;
     else if (n == "tensor_cores") *value = c->tc_option;
     else if (n == "df_products") *value = c->df_option;
     else if (n == "df_rows") *value = c->df_rows;
@@ -3270,6 +3334,7 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     else if (n == "internal_f") *value = c->internal_f_option;
     else if (n == "sched.df_fwd") *value = c->df_fwd;
     else if (n == "sched.df_trans") *value = c->df_trans;
+    else if (n == "sched.tc_screen") *value = (s.tc && c->tc_ready && c->tc_screen_option != 0) ? 1 : 0;
     else if (n == "graphs.captured") *value = (int64_t)c->graphs.size();
     else throw pqdts::Err(PQDTS_E_ARG, "unknown option " + n);
   });
@@ -3291,10 +3356,11 @@ int pqdts_cuda_timer(pqdts_ctx* c, const char* name, double* seconds, int64_t* c
 
 // Tasks of a batched solve: single instances, and groups of instances that
 // share F (the same M, N, D and bands and values) solved in lockstep with a
-// joint CG (mixed precision, mode 2, 32 <= N <= 1024; at most kGroupMax
+// joint CG (mixed precision, mode 2, N <= kGroupMaxN; at most kGroupMax
 // members and M*G*N < 2^31 per group).  PQDTS_BATCH_GROUPS=0 turns the
 // grouping off.
 static constexpr int kGroupMax = 16;
+static constexpr int64_t kGroupMaxN = 4096;
 
 static std::vector<std::vector<int>> batch_tasks(int n_inst, const int64_t* M, const int64_t* N, const int64_t* D,
                                                  const int64_t* band_lo, const int64_t* band_hi,
@@ -3347,7 +3413,7 @@ static std::vector<std::vector<int>> batch_tasks(int n_inst, const int64_t* M, c
         taken[j] = 1;
       }
     const int64_t cap = std::max<int64_t>(1, std::min<int64_t>(kGroupMax, (((int64_t)1 << 31) - 1) / (M[k] * N[k])));
-    const bool joint = grp.size() >= 2 && N[k] >= 32 && N[k] <= 1024 && cap >= 2;
+    const bool joint = grp.size() >= 2 && N[k] <= kGroupMaxN && cap >= 2;
     if (!joint) {
       for (int j : grp) tasks.push_back({j});
       continue;

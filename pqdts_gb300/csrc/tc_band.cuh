@@ -647,6 +647,38 @@ __global__ void k_split_t(const float* __restrict__ V, int M, int N, int64_t ld,
   }
 }
 
+// Line-search probes -> the K-major split operand of their F products:
+// probe b = blockIdx.z, dX = (float)(Xc[b] - X0) (M x N, FP64 in), written
+// transposed as rows b * N + n of hi / lo (hi[(b * N + n) * ld + i]), so one
+// tensor-core product over N' = nb * N columns gives F.dX of every probe.
+__global__ void k_delta_split_t(const double* __restrict__ Xc, const double* __restrict__ X0, int M, int N,
+                                int64_t ld, __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
+  __shared__ float t[32][33];
+  const int b = blockIdx.z;
+  const double* x = Xc + (int64_t)b * M * N;
+  const int i0 = blockIdx.x * 32, n0 = blockIdx.y * 32;
+  for (int rr = threadIdx.y; rr < 32; rr += blockDim.y) {
+    const int i = i0 + rr, n = n0 + threadIdx.x;
+    float v = 0.f;
+    if (i < M && n < N) {
+      const int64_t k = (int64_t)i * N + n;
+      v = (float)(x[k] - X0[k]);
+    }
+    t[rr][threadIdx.x] = v;
+  }
+  __syncthreads();
+  const int64_t row0 = (int64_t)b * N;
+  for (int rr = threadIdx.y; rr < 32; rr += blockDim.y) {
+    const int n = n0 + rr, i = i0 + threadIdx.x;
+    if (n < N && i < M) {
+      const float v = t[threadIdx.x][rr];
+      const __nv_bfloat16 h = __float2bfloat16_rn(v);
+      hi[(row0 + n) * ld + i] = h;
+      lo[(row0 + n) * ld + i] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
+  }
+}
+
 // Tensor-core mixed CG, one launch before the Hessian product: the p update
 // p = beta p + z (2075; skipped when do_update = 0, the first iteration),
 // then V = p, or in the reduced space BF's lift (260-267) V = p with entry

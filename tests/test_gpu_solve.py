@@ -123,9 +123,12 @@ def test_batch_matches_single(built):
 
 def test_batch_groups_lockstep(built, monkeypatch):
     """Mixed-precision instances that share F (resampled P, a gamma sweep)
-    are solved in lockstep groups with a joint CG: every instance reaches its
-    FP64 objective (conv < 1e-9 pins it) to 1e-8 relative, Pi >= 0 exactly,
-    as the same batch does with the grouping off."""
+    are solved in lockstep groups with a joint CG: every instance whose FP64
+    solve reaches conv < 1e-9 (which pins the objective) is matched to 1e-8
+    relative, and every instance ends feasible with Pi >= 0 exactly, as the
+    same batch does with the grouping off.  (Members 0 and 3 of this batch
+    crawl in stage 2 and stop at the iteration limit with conv ~1e-7 in
+    FP64, so their objectives are not pinned.)"""
     import pqdts_gb300 as pq
     from pqdts_gb300 import synth
 
@@ -134,11 +137,14 @@ def test_batch_groups_lockstep(built, monkeypatch):
     assert list(groups) == [0, 0, 0, 1, 1, 1]
     _, st64 = pq.solve_batch(insts, precision=pq.FP64, maxiter=2000, eps=1e-9)
     L64 = np.array([x["L"] for x in st64])
+    pinned = [x["conv"] <= 1e-9 for x in st64]
+    assert sum(pinned[:3]) >= 2 and sum(pinned[3:]) >= 2, st64  # both groups hold pinned members
     for flag in ("1", "0"):
         monkeypatch.setenv("PQDTS_BATCH_GROUPS", flag)
         Xm, sm = pq.solve_batch(insts, precision=pq.MIXED, maxiter=2000, eps=1e-9)
-        for X, st, l64 in zip(Xm, sm, L64):
-            assert abs(st["L"] - l64) <= MIXED_OBJ_REL * abs(l64), (flag, st, l64)
+        for X, st, l64, pin in zip(Xm, sm, L64, pinned):
+            if pin:
+                assert abs(st["L"] - l64) <= MIXED_OBJ_REL * abs(l64), (flag, st, l64)
             _feasible(X, exact=True)
     # the benchmark's stopping rule: each member stops at its own target
     monkeypatch.setenv("PQDTS_BATCH_GROUPS", "1")

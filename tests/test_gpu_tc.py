@@ -80,9 +80,12 @@ def test_tc_hessian_product_matches_fp64(built, tc_insts, which, full, persisten
 
 
 @pytest.mark.parametrize("persistent", [0, 1])
-def test_tc_mixed_solve_reaches_fp64_objective(built, tc_insts, persistent):
+@pytest.mark.parametrize("screen", [0, 1])
+def test_tc_mixed_solve_reaches_fp64_objective(built, tc_insts, persistent, screen):
     """The mixed solve with tensor-core CG products ends within 1e-8 of the
-    FP64 solve's objective (conv < 1e-9 pins it), feasible."""
+    FP64 solve's objective (conv < 1e-9 pins it), feasible -- with the line
+    search's probe products F.dX on the tensor cores (screen = 1: one
+    split-BF16x3 product over all probes' columns) or on the CUDA cores."""
     import pqdts_gb300 as pq
 
     inst = tc_insts["cfg1"]
@@ -90,6 +93,8 @@ def test_tc_mixed_solve_reaches_fp64_objective(built, tc_insts, persistent):
         s64.set_instance(inst, pq.FP64)
         st64 = s64.solve(mode=2, maxiter=2000, eps=1e-9)
     s = _tc_solver(inst, persistent)
+    s.set_option("tc_screen", screen)
+    assert s.get_option("sched.tc_screen") == screen
     st = s.solve(mode=2, maxiter=2000, eps=1e-9)
     X = s.get_x()
     s.close()

@@ -89,7 +89,7 @@ def test_run_pqdts_dry_run_needs_no_gpu():
 
 def test_batch_groups_host_only(built):
     """The batch's lockstep grouping is a host computation: instances with
-    identical F (and 32 <= N <= 1024) share a group, others are alone."""
+    identical F (and N <= 4096) share a group, others are alone."""
     import dataclasses
 
     import pqdts_gb300 as pq
@@ -102,6 +102,8 @@ def test_batch_groups_host_only(built):
     v[5] *= 1.0 + 1e-15
     changed = insts[:3] + [dataclasses.replace(insts[1], band_val=v)]
     assert list(pq.batch_groups(changed)) == [0, 0, 0, -1]
-    # N below a warp: solved alone
+    # small N groups too; N above 4096 is solved alone
     small = synth.make_batch(n_base=1, n_resample=3, shots=10**6, seed=4, m_range=(40, 90), n_range=(5, 12))
-    assert list(pq.batch_groups(small)) == [-1, -1, -1]
+    assert list(pq.batch_groups(small)) == [0, 0, 0]
+    wide = [dataclasses.replace(i, N=5000, P=np.zeros((i.D, 5000))) for i in small]
+    assert list(pq.batch_groups(wide)) == [-1, -1, -1]
