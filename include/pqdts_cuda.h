@@ -68,6 +68,11 @@ int pqdts_cuda_kernel_launches(pqdts_ctx* ctx, int64_t* count);
  *              form (one CTA per output tile, or persistent with
  *              double-buffered accumulators); "tc_splits1" -1 (autotuned) or
  *              1..8: K segments of the tensor-core F.V product.
+ *   "tc_screen" -1 (default) / 0: the mixed line search's probe products
+ *              F.dX (its screen of step lengths, before the chosen step's
+ *              double-FP32 check) as one tensor-core product over all
+ *              probes' columns wherever the CG's products run on the tensor
+ *              cores; 0: FP32 CUDA-core tiles.
  *   "df_products" -1 (default, auto) / 1: the mixed path's gradient F^T.R
  *              and its objective checks (residual F.X - P) in double-FP32
  *              (pairs of FP32 numbers, ~sqrt(K) * 2^-48 relative to the
@@ -106,7 +111,8 @@ int pqdts_cuda_set_option(pqdts_ctx* ctx, const char* name, int64_t value);
  * "sched.tc_splits" (K segments of their F^T product), "sched.tc_splits1"
  * (of their F.V product), "sched.tc_persistent" (kernel form),
  * "sched.df_fwd", "sched.df_trans" (double-FP32 residual / gradient
- * products in use), "graphs.captured" (graphs held). */
+ * products in use), "sched.tc_screen" (line-search probe products on the
+ * tensor cores), "graphs.captured" (graphs held). */
 int pqdts_cuda_get_option(pqdts_ctx* ctx, const char* name, int64_t* value);
 /* verbose = 1 prints the reference's stdout lines (iter, newton-pcg, line
  * search, positivity constraints) exactly as rank 0 of pqdts_omp.x. */

@@ -620,6 +620,7 @@ static void setup_device(Ctx& c) {
   c.cg64.alloc(MN, M, D * N);
   c.sqd.alloc(M);
   CK(cudaFuncSetAttribute(k_condat_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCondatSmemMax));
+  CK(cudaFuncSetAttribute(k_simplex_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCondatSmemMax));
   c.counters.alloc(8);
   CK(cudaMemsetAsync(c.counters.p, 0, 8 * sizeof(unsigned), c.st));
   c.exact = (c.precision == PQDTS_FP64);
@@ -1648,7 +1649,14 @@ static void project_rows(Ctx& c, const double* X, const double* S, const double*
       k_condat<<<dim3(cdiv(M, kRowThreads), B), kRowThreads, 0, c.st>>>(X, S, alphas, out, c.aux.p, MN, M, N);
     }
   } else {
-    k_simplex<<<dim3(cdiv((int64_t)M * 32, 128), B), 128, 0, c.st>>>(X, S, alphas, out, MN, M, N);
+    // rows staged in shared memory: up to 4 warps (rows) per block
+    const int wpb = (int)std::min<int64_t>(4, (int64_t)kCondatSmemMax / ((int64_t)N * 8));
+    if (wpb >= 1) {
+      k_simplex_smem<<<dim3(cdiv(M, wpb), B), 32 * wpb, (size_t)wpb * N * sizeof(double), c.st>>>(X, S, alphas, out,
+                                                                                                 MN, M, N);
+    } else {
+      k_simplex<<<dim3(cdiv((int64_t)M * 32, 128), B), 128, 0, c.st>>>(X, S, alphas, out, MN, M, N);
+    }
   }
   post_launch(c);
 }
@@ -2451,8 +2459,10 @@ static void tune_schedule(Ctx& c, Schedule& s) {
   const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
   const int64_t MN = (int64_t)M * N;
   // FP64 transposed product: for each column count C, the thread count with
-  // the fewest passes over the CSR row, then the fewest idle lanes
-  {
+  // the fewest passes over the CSR row, then the fewest idle lanes (not for
+  // a mixed problem whose gradient and checks run in double-FP32: there the
+  // FP64 products serve only the final refinement, on heuristic shapes)
+  if (c.precision != PQDTS_MIXED || !(c.df_fwd && c.df_trans)) {
     CGBufs<double>& b = c.cg64;
     CK(cudaMemsetAsync(b.R2.p, 0, b.R2.n * sizeof(double), c.st));
     CK(cudaMemsetAsync(b.p.p, 0, b.p.n * sizeof(double), c.st));

@@ -81,13 +81,20 @@ def test_reference_condat_symbol_threads(built):
         assert np.array_equal(x, condat(r))
 
 
-@pytest.mark.parametrize("which", ["cfg1", "small", "mid"])
+@pytest.mark.parametrize("which", ["cfg1", "small", "mid", "wide"])
 def test_mixed_projection_matches_condat(built, request, which):
-    """doproj on a mixed problem runs k_simplex (one warp per row)."""
+    """doproj on a mixed problem runs the warp-per-row projection (rows
+    staged in shared memory, Michelot's iteration on a shrinking active
+    list); wide: N = 1500 rows (47 entries per lane, 4 rows per block)."""
     import pqdts_gb300 as pq
     from oracle.oracle import condat
+    from pqdts_gb300 import synth
 
-    inst = request.getfixturevalue(which)
+    if which == "wide":
+        inst = synth.make_instance(M=70, N=1500, D=140, xmax=60.0, eta=0.85, shots=10**5, gamma=1e-4, eps=1e-6,
+                                   seed=1)
+    else:
+        inst = request.getfixturevalue(which)
     rng = np.random.default_rng(23)
     Y = np.asfortranarray(rng.standard_normal((inst.M, inst.N)) * 0.7 + 0.05)
     with pq.Solver(0) as s:
