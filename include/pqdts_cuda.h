@@ -265,7 +265,7 @@ int pqdts_cuda_timer(pqdts_ctx* ctx, const char* name, double* seconds, int64_t*
  * order, so tasks overlap on the device; each context's CG chunks replay as
  * CUDA graphs and instances of one size bucket share one autotuned launch
  * schedule.  A task is one instance, or (PQDTS_MIXED, mode 2, N <= 4096)
- * a group of up to 16 instances with the same M, N, D and identical F
+ * a group of up to 4 instances with the same M, N, D and identical F
  * (bands and values: resampled P, gamma sweeps), solved in lockstep: each
  * member keeps its own line search and stages, and their FP32 CG runs
  * jointly -- every CG launch serves all members, the tensor-core products
