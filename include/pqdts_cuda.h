@@ -264,13 +264,15 @@ int pqdts_cuda_timer(pqdts_ctx* ctx, const char* name, double* seconds, int64_t*
  * most one per task) each own a context and stream and take tasks in
  * order, so tasks overlap on the device; each context's CG chunks replay as
  * CUDA graphs and instances of one size bucket share one autotuned launch
- * schedule.  A task is one instance, or (PQDTS_MIXED, mode 2, N <= 4096)
- * a group of up to 4 instances with the same M, N, D and identical F
- * (bands and values: resampled P, gamma sweeps), solved in lockstep: each
- * member keeps its own line search and stages, and their FP32 CG runs
- * jointly -- every CG launch serves all members, the tensor-core products
- * taking the members' vectors as the columns of one wider product.  The
- * environment variable PQDTS_BATCH_GROUPS=0 turns the grouping off. */
+ * schedule.  A task is one instance, or, when the environment variable
+ * PQDTS_BATCH_GROUPS=1 turns the grouping on (PQDTS_MIXED, mode 2,
+ * N <= 4096), a group of up to 4 instances with the same M, N, D and
+ * identical F (bands and values: resampled P, gamma sweeps), solved in
+ * lockstep: each member keeps its own line search and stages, and their
+ * FP32 CG runs jointly -- every CG launch serves all members, the
+ * tensor-core products taking the members' vectors as the columns of one
+ * wider product.  Off by default: independent solves were faster on the
+ * 64-instance batch (5.0 s against 6.4 s). */
 int pqdts_cuda_solve_batch(int32_t device, int32_t n_inst, const int64_t* M, const int64_t* N, const int64_t* D,
                            const int64_t* band_lo, const int64_t* band_hi, const double* band_vals,
                            const int64_t* band_row_offset, const int64_t* band_val_offset, const double* P,
@@ -278,7 +280,8 @@ int pqdts_cuda_solve_batch(int32_t device, int32_t n_inst, const int64_t* M, con
                            int32_t maxiiter, double conv_thres, const double* target_L, double* X, double* stats);
 
 /* The grouping pqdts_cuda_solve_batch uses for a mixed-precision mode-2
- * batch (same arguments as there): group_of[k] = the group of instance k
+ * batch when PQDTS_BATCH_GROUPS=1 (same arguments as there): group_of[k] =
+ * the group of instance k
  * (instances solved in lockstep with a joint CG) or -1 (solved alone).  Host
  * only, needs no device.  No counterpart in the reference. */
 int pqdts_cuda_batch_groups(int32_t n_inst, const int64_t* M, const int64_t* N, const int64_t* D,

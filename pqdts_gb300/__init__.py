@@ -331,8 +331,9 @@ def batch_groups(instances):
 def solve_batch(instances, X0=None, precision=FP64, mode=2, maxiter=100, eps=1e-6, device=0, targets=None):
     """Solve independent instances (uneven M, N, D, gamma) on one GPU;
     `targets`: optional per-instance objective targets (stop once L <= it).
-    Mixed-precision instances that share F are solved in lockstep groups
-    with a joint CG (batch_groups shows the grouping)."""
+    With the environment variable PQDTS_BATCH_GROUPS=1, mixed-precision
+    instances that share F are solved in lockstep groups with a joint CG
+    (batch_groups shows the grouping); off by default."""
     L = lib()
     k = len(instances)
     M, N, D, lo, hi, vals, row_off, val_off = _batch_arrays(instances)

@@ -48,7 +48,6 @@ template <int Y>
 __global__ void __launch_bounds__(32 * Y) k_cg_lift_split_b(const CGMember* __restrict__ mem, int do_update, int M,
                                                             int N, int64_t ld, __nv_bfloat16* __restrict__ hi,
                                                             __nv_bfloat16* __restrict__ lo) {
-  pdl_enter();
   const CGMember& m = mem[blockIdx.y];
   if (!m.active || m.sc[SC_DONE] != 0.0) return;
   const int64_t off = (int64_t)blockIdx.y * N * ld;
@@ -60,7 +59,6 @@ __global__ void __launch_bounds__(32 * Y) k_cg_lift_split_b(const CGMember* __re
 __global__ void __launch_bounds__(256) k_hvp_epi32_rows_b(const CGMember* __restrict__ mem,
                                                          const float* __restrict__ Hraw, int64_t hstride,
                                                          int64_t hplane, int M, int N, int RB, int parts) {
-  pdl_enter();
   const CGMember& m = mem[blockIdx.y];
   if (!m.active || m.sc[SC_DONE] != 0.0) return;
   hvp_epi32_rows_body(blockIdx.x, gridDim.x, Hraw + (int64_t)blockIdx.y * N, hstride, hplane, m.p, m.rs, m.maxr,
@@ -68,7 +66,6 @@ __global__ void __launch_bounds__(256) k_hvp_epi32_rows_b(const CGMember* __rest
 }
 
 __global__ void k_cg_step32_b(const CGMember* __restrict__ mem, CGGroup grp, int M, int N, int maxit) {
-  pdl_enter();
   const CGMember& m = mem[blockIdx.y];
   if (!m.active || m.sc[SC_DONE] != 0.0) return;
   const bool advanced = cg_step32_body(blockIdx.x, gridDim.x, m.sc, m.rsq, M, N, m.p, m.Hp, m.sn, m.r, m.z,

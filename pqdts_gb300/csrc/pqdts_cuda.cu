@@ -409,7 +409,6 @@ struct pqdts_ctx {
   const void* ls_map_ptr = nullptr;
   int64_t ls_map_mp = 0, ls_map_rows = 0;
   int tc_screen_option = -1;  // line-search screen on the tensor cores: -1 auto (with the CG's), 0 off
-  int pdl_option = -1;        // programmatic dependent launch in CG iterations: -1 auto, 0 off
   pqdts::Schedule sched;
   bool own_stream = true;  // false: a member of a batched group, on the group's stream
   // group context of a batched lockstep solve: the members' CG table
@@ -488,29 +487,6 @@ static void touch_x(Ctx& c) { c.xver++; }
 static void post_launch(Ctx& c) {
   c.launches++;
   CK(cudaGetLastError());
-}
-
-// Programmatic dependent launch for the kernels of a CG iteration (each of
-// them waits for its predecessor in pdl_enter): on unless the option is 0
-// or the region timers record events between the kernels.
-static bool use_pdl(const Ctx& c) { return c.pdl_option != 0 && !c.timers.enabled; }
-
-// kern<<<grid, block, smem, c.st>>>(args...), with the programmatic-
-// serialization attribute when pdl is set.
-template <typename... KArgs, typename... Args>
-static void launch_k(Ctx& c, bool pdl, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, Args&&... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = c.st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = pdl ? 1 : 0;
-  CK(cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...));
-  post_launch(c);
 }
 
 static int elem_grid(int64_t total) { return std::max(1, std::min<int>(kElemGrid, cdiv(total, 256))); }
@@ -1211,18 +1187,19 @@ static void tc_product(Ctx& c, TcOperand& A, const CUtensorMap& bhi, const CUten
                        const double* pred, int persistent, int Nw = -1) {
   const int N = Nw > 0 ? Nw : (int)c.h.N;
   const size_t smem = (size_t)c.tc_stages * tc_stage_bytes(c.tc_bn) + 1024;
-  const bool pdl = pred != nullptr && use_pdl(c);  // inside a CG iteration
   if (persistent) {
     TcSched& ts = tc_sched(c, A, c.tc_bn, splits, N);
-    launch_k(c, pdl, k_tc_band_p, dim3(ts.grid), dim3(kTcpThreads), smem, A.map_hi, A.map_lo, bhi, blo, A.kb.p,
-             A.nch.p, R, N, c.tc_bn, c.tc_stages, splits, A.blocks, mode, scale, out, (int64_t)R * N, oh, ol, ld, pred,
-             c.sc.p + SC_TCERR, c.tc_wait_ns, c.tc_wait_probe, ts.off.p, ts.tile.p);
+    k_tc_band_p<<<ts.grid, kTcpThreads, smem, c.st>>>(A.map_hi, A.map_lo, bhi, blo, A.kb.p, A.nch.p, R, N, c.tc_bn,
+                                                      c.tc_stages, splits, A.blocks, mode, scale, out, (int64_t)R * N,
+                                                      oh, ol, ld, pred, c.sc.p + SC_TCERR, c.tc_wait_ns,
+                                                      c.tc_wait_probe, ts.off.p, ts.tile.p);
   } else {
     const dim3 grid(cdiv(N, c.tc_bn), A.blocks, splits);
-    launch_k(c, pdl, k_tc_band, grid, dim3(kTcThreads), smem, A.map_hi, A.map_lo, bhi, blo, A.kb.p, A.nch.p, R, N,
-             c.tc_bn, c.tc_stages, splits, mode, scale, out, (int64_t)R * N, oh, ol, ld, pred, c.sc.p + SC_TCERR,
-             c.tc_wait_ns, c.tc_wait_probe);
+    k_tc_band<<<grid, kTcThreads, smem, c.st>>>(A.map_hi, A.map_lo, bhi, blo, A.kb.p, A.nch.p, R, N, c.tc_bn,
+                                                c.tc_stages, splits, mode, scale, out, (int64_t)R * N, oh, ol, ld, pred,
+                                                c.sc.p + SC_TCERR, c.tc_wait_ns, c.tc_wait_probe);
   }
+  post_launch(c);
 }
 
 // F.V on the tensor cores into the (2 F.V)^T split operand: directly from
@@ -1237,8 +1214,9 @@ static void tc_forward(Ctx& c, int splits1, int persistent, const double* pred) 
   require(c.ypart.p, "F.V partials");
   tc_product(c, c.tcF, c.map_vt_hi, c.map_vt_lo, D, splits1, 0, 2.0f, c.ypart.p, nullptr, nullptr, 0, pred,
              persistent);
-  launch_k(c, pred != nullptr && use_pdl(c), k_finish_t, dim3(cdiv(D, 32), cdiv(N, 32)), dim3(32, 8), 0, c.ypart.p,
-           splits1, D, N, c.tc_dp, c.yt_hi.p, c.yt_lo.p, pred);
+  k_finish_t<<<dim3(cdiv(D, 32), cdiv(N, 32)), dim3(32, 8), 0, c.st>>>(c.ypart.p, splits1, D, N, c.tc_dp, c.yt_hi.p,
+                                                                       c.yt_lo.p, pred);
+  post_launch(c);
 }
 
 // The Hessian product pair on the tensor cores: V -> V^T split, then
@@ -1356,9 +1334,11 @@ static int hvp_epilogue(Ctx& c, const float* p, const float* rs, const int8_t* i
   const int RB = epi_rows(c, M);
   if (c.rows_option != 0) {
     const bool fused = vsum != nullptr && dpart != nullptr;
-    launch_k(c, pred != nullptr && use_pdl(c), k_hvp_epi32_rows, dim3(cdiv(M, RB)), dim3(kEpiThreads), 0,
-             c.hpart32.p, p, rs, c.maxr.p, rs ? 1 : 0, (float)(2.0 * c.h.gam), ik, M, N, RB, Hp, dpart, pred, parts,
-             fused ? vsum : nullptr, fused ? c.counters.p + 4 : nullptr);
+    k_hvp_epi32_rows<<<cdiv(M, RB), kEpiThreads, 0, c.st>>>(c.hpart32.p, p, rs, c.maxr.p, rs ? 1 : 0,
+                                                            (float)(2.0 * c.h.gam), ik, M, N, RB, Hp, dpart, pred,
+                                                            parts, fused ? vsum : nullptr,
+                                                            fused ? c.counters.p + 4 : nullptr);
+    post_launch(c);
     return fused ? 0 : cdiv(M, RB);
   }
   const int tb = std::min(256, std::max(32, cdiv(N, 32) * 32));
@@ -1530,8 +1510,10 @@ static void cg_solve32(Ctx& c, double bdfac) {
       // p update, BF's lift (reduced space: row sums) and the first
       // product's operand split in one launch (no row-major V)
       Scope sd(c.timers, "CG.lift_split", true);
-      launch_k(c, use_pdl(c), k_cg_lift_split<32>, dim3(cdiv(M, 32)), dim3(32, 32), 0, c.sc.p, first ? 0 : 1, M, N,
-               b.p.p, b.z.p, c.fullspace ? nullptr : c.maxr.p, b.rs.p, c.tc_mp, c.vt_hi.p, c.vt_lo.p);
+      k_cg_lift_split<32><<<cdiv(M, 32), dim3(32, 32), 0, c.st>>>(c.sc.p, first ? 0 : 1, M, N, b.p.p, b.z.p,
+                                                              c.fullspace ? nullptr : c.maxr.p, b.rs.p, c.tc_mp,
+                                                              c.vt_hi.p, c.vt_lo.p);
+      post_launch(c);
     } else if (c.fullspace) {
       if (!first) {
         k_cg_pupdate<float><<<g, 256, 0, c.st>>>(c.sc.p, MN, b.p.p, b.z.p);
@@ -1549,8 +1531,9 @@ static void cg_solve32(Ctx& c, double bdfac) {
     // the step (one warp per row); its last block sums r.z, r.r and
     // advances the CG scalars
     Scope sd(c.timers, "CG.step", true);
-    launch_k(c, tc && use_pdl(c), k_cg_step32, dim3(gs), dim3(256), 0, c.sc.p, c.rsq32.p, M, N, b.p.p, b.Hp.p,
-             b.sn.p, b.r.p, b.z.p, c.part.p, c.part2.p, c.cglog.p, kMaxCG, c.counters.p + 1);
+    k_cg_step32<<<gs, 256, 0, c.st>>>(c.sc.p, c.rsq32.p, M, N, b.p.p, b.Hp.p, b.sn.p, b.r.p, b.z.p, c.part.p,
+                                      c.part2.p, c.cglog.p, kMaxCG, c.counters.p + 1);
+    post_launch(c);
   };
   const int done_iters = cg_chunks(c, {0, (uint64_t)c.fullspace, 0, 0}, iteration);
   cg32_end(c, done_iters);
@@ -2346,14 +2329,18 @@ static void group_cg32(Ctx& g, std::vector<MemberRun>& ms, const std::vector<int
   const int RB = epi_rows(g, M);
   const int gs = std::min(elem_grid((int64_t)M * N), cdiv(M, 8));
   auto iteration = [&](bool first) {
-    launch_k(g, use_pdl(g), k_cg_lift_split_b<32>, dim3(cdiv(M, 32), G), dim3(32, 32), 0, g.memtab.p, first ? 0 : 1,
-             M, N, g.tc_mp, g.vt_hi.p, g.vt_lo.p);
+    k_cg_lift_split_b<32><<<dim3(cdiv(M, 32), G), dim3(32, 32), 0, g.st>>>(g.memtab.p, first ? 0 : 1, M, N, g.tc_mp,
+                                                                           g.vt_hi.p, g.vt_lo.p);
+    post_launch(g);
     tc_forward(g, g.sched.tc_splits1, g.sched.tc_persistent, g.sc.p);
     tc_product(g, g.tcFt, g.map_yt_hi, g.map_yt_lo, M, g.sched.tc_splits, 0, 1.0f, g.hpart32.p, nullptr, nullptr, 0,
                g.sc.p, g.sched.tc_persistent);
-    launch_k(g, use_pdl(g), k_hvp_epi32_rows_b, dim3(cdiv(M, RB), G), dim3(kEpiThreads), 0, g.memtab.p, g.hpart32.p,
-             Nw, (int64_t)M * Nw, M, N, RB, g.sched.tc_splits);
-    launch_k(g, use_pdl(g), k_cg_step32_b, dim3(gs, G), dim3(256), 0, g.memtab.p, grp, M, N, kMaxCG);
+    k_hvp_epi32_rows_b<<<dim3(cdiv(M, RB), G), kEpiThreads, 0, g.st>>>(g.memtab.p, g.hpart32.p, Nw,
+                                                                        (int64_t)M * Nw, M, N, RB,
+                                                                        g.sched.tc_splits);
+    post_launch(g);
+    k_cg_step32_b<<<dim3(gs, G), 256, 0, g.st>>>(g.memtab.p, grp, M, N, kMaxCG);
+    post_launch(g);
   };
   cg_chunks(g, {100, (uint64_t)active, 0, 0}, iteration);
   for (int j : in_cg) {
@@ -3294,10 +3281,6 @@ int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
     } else if (n == "tc_screen") {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "tc_screen must be -1, 0 or 1");
       c->tc_screen_option = (int)value;
-    } else if (n == "pdl") {
-      if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "pdl must be -1, 0 or 1");
-      c->pdl_option = (int)value;
-      c->drop_graphs();  // captured CG chunks carry the launch attribute
     } else if (n == "tensor_cores") {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "tensor_cores must be -1, 0 or 1");
       c->tc_option = (int)value;
@@ -3352,8 +3335,6 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     else if (n == "rows_kernels") *value = c->rows_option;
     else if (n == "tc_persistent") *value = c->tc_persistent_option;
     else if (n == "tc_screen") *value = c->tc_screen_option;
-    else if (n == "pdl") *value = c->pdl_option;
-    else if (n == "sched.pdl") *value = pqdts::use_pdl(*c) ? 1 : 0;
     else if (n == "tensor_cores") *value = c->tc_option;
     else if (n == "df_products") *value = c->df_option;
     else if (n == "df_rows") *value = c->df_rows;
@@ -3386,12 +3367,13 @@ int pqdts_cuda_timer(pqdts_ctx* c, const char* name, double* seconds, int64_t* c
 // Tasks of a batched solve: single instances, and groups of instances that
 // share F (the same M, N, D and bands and values) solved in lockstep with a
 // joint CG (mixed precision, mode 2, N <= kGroupMaxN; at most kGroupMax
-// members and M*G*N < 2^31 per group).  PQDTS_BATCH_GROUPS=0 turns the
-// grouping off.  Groups stay small: a group's members take their line
-// searches one after another on the group's worker, so the 64-instance
-// batch (8 detectors x 8 resamples) runs as 16 groups of 4 on 16 workers
-// (as 8 groups of 8 on 8 workers it took 6.9 s against 5.0 s for 64
-// independent solves on 16 workers).
+// members and M*G*N < 2^31 per group), when PQDTS_BATCH_GROUPS=1 turns the
+// grouping on.  It is off by default: a group's members take their line
+// searches one after another on the group's worker and its joint CG runs
+// as long as its slowest member's, and on the 64-instance batch (8
+// detectors x 8 resamples) the groups took 6.4 s (16 groups of 4 on 16
+// workers; 6.9 s as 8 groups of 8) against 5.0 s for 64 independent solves
+// on 16 workers.
 static constexpr int kGroupMax = 4;
 static constexpr int64_t kGroupMaxN = 4096;
 
@@ -3493,8 +3475,8 @@ int pqdts_cuda_solve_batch(int32_t device, int32_t n_inst, const int64_t* M, con
   // context and stream, so the tasks' kernels overlap on the device.
   std::vector<int64_t> xoff(n_inst + 1, 0);
   for (int k = 0; k < n_inst; ++k) xoff[k + 1] = xoff[k] + M[k] * N[k];
-  bool grouping = precision == PQDTS_MIXED && mode == 2;
-  if (const char* e = std::getenv("PQDTS_BATCH_GROUPS")) grouping = grouping && std::atoi(e) != 0;
+  bool grouping = false;
+  if (const char* e = std::getenv("PQDTS_BATCH_GROUPS")) grouping = precision == PQDTS_MIXED && mode == 2 && std::atoi(e) != 0;
   std::vector<std::vector<int>> tasks;
   try {
     tasks = batch_tasks(n_inst, M, N, D, band_lo, band_hi, band_vals, band_row_offset, band_val_offset, grouping);

@@ -178,7 +178,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               int stages, int splits, int mode, float scale, float* __restrict__ out, int64_t out_stride,
               __nv_bfloat16* __restrict__ oh, __nv_bfloat16* __restrict__ ol, int64_t ld,
               const double* __restrict__ pred, double* __restrict__ err, uint64_t wait_ns, int probe) {
-  pdl_enter();
   if (pred != nullptr && pred[6] != 0.0) return;  // CG already converged
   extern __shared__ uint8_t tc_smem_raw[];
   __shared__ uint64_t bar_full[kTcMaxStages], bar_empty[kTcMaxStages], bar_acc, bar_probe;
@@ -385,7 +384,6 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
                 int64_t out_stride, __nv_bfloat16* __restrict__ oh, __nv_bfloat16* __restrict__ ol, int64_t ld,
                 const double* __restrict__ pred, double* __restrict__ err, uint64_t wait_ns, int probe,
                 const int32_t* __restrict__ sched_off, const int32_t* __restrict__ sched_tile) {
-  pdl_enter();
   if (pred != nullptr && pred[6] != 0.0) return;  // CG already converged
   extern __shared__ uint8_t tc_smem_raw[];
   __shared__ uint64_t bar_full[kTcMaxStages], bar_empty[kTcMaxStages], bar_tfull[2], bar_tempty[2], bar_fin,
@@ -596,7 +594,6 @@ __global__ void __launch_bounds__(kTcpThreads, 1)
 __global__ void k_finish_t(const float* __restrict__ part, int parts, int R, int N, int64_t ld,
                            __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
                            const double* __restrict__ pred) {
-  pdl_enter();
   if (pred != nullptr && pred[6] != 0.0) return;
   __shared__ float t[32][33];
   const int r0 = blockIdx.x * 32, n0 = blockIdx.y * 32;
@@ -785,7 +782,6 @@ __global__ void __launch_bounds__(32 * Y) k_cg_lift_split(const double* __restri
                                                           const int32_t* __restrict__ maxr, float* __restrict__ rs,
                                                           int64_t ld, __nv_bfloat16* __restrict__ hi,
                                                           __nv_bfloat16* __restrict__ lo) {
-  pdl_enter();
   if (sc != nullptr && sc[SC_DONE] != 0.0) return;
   cg_lift_split_body<Y>(blockIdx.x, sc, do_update, M, N, p, z, maxr, rs, ld, hi, lo);
 }
