@@ -1459,16 +1459,16 @@ static void cg32_begin(Ctx& c, double bdfac) {
   const int g = elem_grid(MN);
   CGBufs<float>& b = c.cg32;
   require(c.tbval32.p, "F^T band values (FP32)");
-  k_cg_init<float><<<g, 256, 0, c.st>>>(c.X.p, c.G.p, c.bdiag.p, bdfac, kActiveTol, M, N, c.ik.p, b.r.p, b.z.p, b.p.p,
-                                        b.sn.p, c.part.p, c.part2.p, c.ipart.p);
+  k_rsqrt_diag<<<cdiv(M, 256), 256, 0, c.st>>>(c.bdiag.p, bdfac, M, c.rsq32.p);
+  post_launch(c);
+  k_cg_init32<<<g, 256, 0, c.st>>>(c.X.p, c.G.p, c.rsq32.p, kActiveTol, M, N, c.ik.p, b.r.p, b.z.p, b.p.p, b.sn.p,
+                                   c.part.p, c.part2.p, c.ipart.p);
   post_launch(c);
   reduce_to(c, c.part.p, g, c.sc.p + SC_NORM);
   reduce_to(c, c.part2.p, g, c.sc.p + SC_RZ);
   k_sum_i<<<1, 256, 0, c.st>>>(c.ipart.p, g, c.icount.p);
   post_launch(c);
   k_cg_scalars0<<<1, 1, 0, c.st>>>(c.sc.p);
-  post_launch(c);
-  k_rsqrt_diag<<<cdiv(M, 256), 256, 0, c.st>>>(c.bdiag.p, bdfac, M, c.rsq32.p);
   post_launch(c);
   if (c.verbose) {
     long long nact = 0;
@@ -1976,7 +1976,7 @@ static void outer_post_cg(Ctx& c, SolveState& st, double bdfac, bool fp32) {
   if (c.precision == PQDTS_MIXED && c.refine) c.n_refine++;
   op_dL(c);
   const int32_t* mr = c.fullspace ? nullptr : c.maxr.p;
-  if (fp32) k_twometric<float><<<g, 256, 0, c.st>>>(c.cg32.sn.p, c.G.p, c.ik.p, mr, c.bdiag.p, bdfac, M, N, c.sn64.p);
+  if (fp32) k_twometric32<<<g, 256, 0, c.st>>>(c.cg32.sn.p, c.G.p, c.ik.p, mr, c.bdiag.p, bdfac, M, N, c.sn64.p);
   else k_twometric<double><<<g, 256, 0, c.st>>>(c.cg64.sn.p, c.G.p, c.ik.p, mr, c.bdiag.p, bdfac, M, N, c.sn64.p);
   post_launch(c);
   if (c.exact) line_search(c, !c.fullspace, st.alpha, st.dlalpha);
