@@ -353,10 +353,6 @@ struct pqdts_ctx {
   // objective checks (option -1 auto = on, 0 native FP64, 1 on): F and F^T
   // values, and the split X and R operands, as (hi, lo) pairs
   pqdts::DBuf<float2> fdf, tdf, xdf, rdf;
-  // rows of the double-FP32 products' operand that can be non-zero, per
-  // group of 32 columns (k_split_df_support), and whether they are used
-  pqdts::DBuf<int> supp_lo, supp_hi;
-  int df_skip_option = 1;
   int df_option = -1;
   int df_rows = 0;  // band rows per block of the double-FP32 products (0: chosen by size)
   bool df_fwd = false, df_trans = false;
@@ -533,37 +529,16 @@ static int df_rows_per_block(int64_t rows, int N, int rbopt, int sms) {
   return 2;
 }
 
-// src (rows x N, FP64) -> its double-FP32 split dst; with the option
-// df_skip (default) also the rows each group of 32 columns can be non-zero
-// in (c.supp_lo / supp_hi), which the products then skip outside; returns
-// them, or nulls.
-static std::pair<const int*, const int*> split_df_operand(Ctx& c, const double* src, int64_t rows, float2* dst) {
-  const int N = (int)c.h.N;
-  if (c.df_skip_option == 0) {
-    k_split_df<<<elem_grid(rows * N), 256, 0, c.st>>>(src, rows * N, 1.0, dst);
-    post_launch(c);
-    return {nullptr, nullptr};
-  }
-  const int ng = cdiv(N, 32);
-  if (c.supp_lo.p == nullptr) throw Err(PQDTS_E_STATE, "internal: operand support not allocated");
-  CK(cudaMemsetAsync(c.supp_lo.p, 0x7f, ng * sizeof(int), c.st));  // 0x7f7f7f7f: above any row
-  CK(cudaMemsetAsync(c.supp_hi.p, 0xff, ng * sizeof(int), c.st));  // -1: no non-zero yet
-  const int gy = (int)std::max<int64_t>(1, std::min<int64_t>(cdiv(rows, 8), cdiv(4 * std::max(c.num_sms, 1), ng)));
-  k_split_df_support<<<dim3(ng, gy), dim3(32, 8), 0, c.st>>>(src, (int)rows, N, dst, c.supp_lo.p, c.supp_hi.p);
-  post_launch(c);
-  return {c.supp_lo.p, c.supp_hi.p};
-}
-
 template <int MODE>
-static void launch_fwd_df(Ctx& c, double* R, const int* slo, const int* shi) {
+static void launch_fwd_df(Ctx& c, double* R) {
   const int N = (int)c.h.N, D = (int)c.h.D;
   const int rb = df_rows_per_block(D, N, c.df_rows, c.num_sms);
   const dim3 grid(cdiv(D, rb), cdiv(N, 32 * kDfColWarps));
   const int threads = 32 * std::min(kDfColWarps, cdiv(N, 32));
   DevBands bd = bands_of(c);
-  if (rb == 8) k_fwd_df<MODE, 8><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R, slo, shi);
-  else if (rb == 4) k_fwd_df<MODE, 4><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R, slo, shi);
-  else k_fwd_df<MODE, 2><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R, slo, shi);
+  if (rb == 8) k_fwd_df<MODE, 8><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R);
+  else if (rb == 4) k_fwd_df<MODE, 4><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R);
+  else k_fwd_df<MODE, 2><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R);
   post_launch(c);
 }
 
@@ -618,8 +593,6 @@ static void setup_device(Ctx& c) {
       for (size_t k = 0; k < fd.size(); ++k) fd[k] = split_df_host(h.fval[k]);
       c.fdf.upload(fd.data(), fd.size(), c.st, &c.h2d);
       c.xdf.alloc(MN);
-      c.supp_lo.alloc((size_t)cdiv(N, 32));
-      c.supp_hi.alloc((size_t)cdiv(N, 32));
     } else {
       c.fdf.release();
       c.xdf.release();
@@ -782,8 +755,9 @@ template <int MODE>
 static void fwd_df(Ctx& c, const double* X, double* R) {
   const int64_t MN = c.h.M * c.h.N;
   require(c.xdf.p, "xdf");
-  const auto sp = split_df_operand(c, X, c.h.M, c.xdf.p);
-  launch_fwd_df<MODE>(c, R, sp.first, sp.second);
+  k_split_df<<<elem_grid(MN), 256, 0, c.st>>>(X, MN, 1.0, c.xdf.p);
+  post_launch(c);
+  launch_fwd_df<MODE>(c, R);
 }
 
 static void objective_stack(Ctx& c, const double* Xs, int B) {
@@ -936,19 +910,17 @@ static void op_dL(Ctx& c) {
     // the reduced one from it
     ensure_R(c);
     const int D = (int)c.h.D;
-    const auto sp = split_df_operand(c, c.R.p, D, c.rdf.p);
+    k_split_df<<<elem_grid((int64_t)D * N), 256, 0, c.st>>>(c.R.p, (int64_t)D * N, 1.0, c.rdf.p);
+    post_launch(c);
     double* g = c.fullspace ? c.G.p : nullptr;
     const double c2g = 2.0 * c.h.gam;
     const int rb = df_rows_per_block(M, N, c.df_rows, c.num_sms);
     const dim3 grid(cdiv(M, rb), cdiv(N, 32 * kDfColWarps));
     const int threads = 32 * std::min(kDfColWarps, cdiv(N, 32));
     DevBands bd = bands_of(c);
-    if (rb == 8)
-      k_trans_df<8><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p, sp.first, sp.second);
-    else if (rb == 4)
-      k_trans_df<4><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p, sp.first, sp.second);
-    else
-      k_trans_df<2><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p, sp.first, sp.second);
+    if (rb == 8) k_trans_df<8><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
+    else if (rb == 4) k_trans_df<4><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
+    else k_trans_df<2><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
     post_launch(c);
     if (!c.fullspace) {
       k_reduced_from_full<<<M, std::min(256, std::max(32, cdiv(N, 32) * 32)), 0, c.st>>>(c.Gf.p, c.maxr.p, N, c.G.p);
@@ -3306,9 +3278,6 @@ int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
     } else if (n == "tc_persistent") {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "tc_persistent must be -1, 0 or 1");
       c->tc_persistent_option = (int)value;
-    } else if (n == "df_skip") {
-      if (value < 0 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "df_skip must be 0 or 1");
-      c->df_skip_option = (int)value;
     } else if (n == "tc_screen") {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "tc_screen must be -1, 0 or 1");
       c->tc_screen_option = (int)value;
@@ -3366,7 +3335,6 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     else if (n == "rows_kernels") *value = c->rows_option;
     else if (n == "tc_persistent") *value = c->tc_persistent_option;
     else if (n == "tc_screen") *value = c->tc_screen_option;
-    else if (n == "df_skip") *value = c->df_skip_option;
     else if (n == "tensor_cores") *value = c->tc_option;
     else if (n == "df_products") *value = c->df_option;
     else if (n == "df_rows") *value = c->df_rows;

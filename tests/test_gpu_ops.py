@@ -271,62 +271,3 @@ def test_L_dL_double_float(built, request, which, full):
     err = np.max(np.abs(G - Go)) / np.max(np.abs(Go))
     assert err < 1e-11, err
     s.close()
-
-
-def _banded_x(inst, seed, half=2):
-    """A feasible X that is exactly zero outside a band in (i, n) plus the
-    last column: the shape of a tomography iterate (outcome n reached from
-    photon numbers near n / eta, the tail mass in the last column)."""
-    rng = np.random.default_rng(seed)
-    M, N = inst.M, inst.N
-    X = np.zeros((M, N))
-    for i in range(M):
-        c = min(N - 1, int(0.6 * i * N / M))
-        lo, hi = max(0, c - half), min(N, c + half + 1)
-        X[i, lo:hi] = rng.random(hi - lo)
-        X[i, N - 1] = rng.random()
-    return np.asfortranarray(X / X.sum(1, keepdims=True))
-
-
-@pytest.mark.parametrize("which", ["cfg1", "wide", "banded"])
-@pytest.mark.parametrize("full", [True, False])
-def test_double_float_zero_skipping(built, request, which, full):
-    """The double-FP32 products skip the operand rows where a group of 32
-    columns is exactly zero (the support found while splitting the
-    operand): the same L and dL as the dense products (the skipped terms are
-    exact zeros; only the points where the pairs renormalise move) and the
-    oracle's to the double-FP32 bound."""
-    import pqdts_gb300 as pq
-    from oracle.oracle import Oracle
-
-    from pqdts_gb300 import synth
-
-    if which == "banded":  # 7 groups of 32 columns, each non-zero on a few dozen rows
-        inst = synth.make_instance(M=300, N=200, D=600, xmax=250.0, eta=0.8, shots=10**6, gamma=1e-4, eps=1e-6, seed=8)
-    else:
-        inst = _df_instances()[which] if which == "wide" else request.getfixturevalue(which)
-    X = _banded_x(inst, 5)
-    assert np.mean(X == 0.0) > 0.5
-    m = None if full else _maxr(X)
-    out = {}
-    for skip in (1, 0):
-        s = pq.Solver(0)
-        s.set_option("df_products", 1)
-        s.set_option("df_skip", skip)
-        s.set_instance(inst, pq.MIXED)
-        assert s.get_option("df_skip") == skip
-        s.set_space(full, m)
-        s.set_x(X)
-        L = s.L()
-        s.set_x(X)
-        out[skip] = (L, s.dL())
-        s.close()
-    o = Oracle.from_instance(inst)
-    o.set_space(full, m)
-    Lo, _ = o.L(X)
-    Go, _ = o.dL(X)
-    (L1, G1), (L0, G0) = out[1], out[0]
-    assert abs(L1 - L0) <= 1e-14 * abs(L0), (L1, L0)
-    assert np.max(np.abs(G1 - G0)) <= 1e-13 * np.max(np.abs(G0))
-    assert abs(L1 - Lo) <= 1e-12 * abs(Lo)
-    assert np.max(np.abs(G1 - Go)) / np.max(np.abs(Go)) < 1e-11
