@@ -353,6 +353,12 @@ struct pqdts_ctx {
   // objective checks (option -1 auto = on, 0 native FP64, 1 on): F and F^T
   // values, and the split X and R operands, as (hi, lo) pairs
   pqdts::DBuf<float2> fdf, tdf, xdf, rdf;
+  // row-occupancy masks of the FP64 forward products' operand (k_row_masks,
+  // up to kBatchLS stacked inputs) and whether they are used: on unless the
+  // option row_masks is 0 or F holds a value that is not finite
+  pqdts::DBuf<uint32_t> xmask;
+  int mask_option = 1;
+  bool f_finite = true;
   int df_option = -1;
   int df_rows = 0;  // band rows per block of the double-FP32 products (0: chosen by size)
   bool df_fwd = false, df_trans = false;
@@ -619,6 +625,8 @@ static void setup_device(Ctx& c) {
   }
   c.cg64.alloc(MN, M, D * N);
   c.sqd.alloc(M);
+  c.f_finite = std::all_of(h.fval.begin(), h.fval.end(), [](double v) { return std::isfinite(v); });
+  c.xmask.alloc((size_t)kBatchLS * cdiv(N, 32) * cdiv(M, 32));
   CK(cudaFuncSetAttribute(k_condat_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCondatSmemMax));
   CK(cudaFuncSetAttribute(k_simplex_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCondatSmemMax));
   c.counters.alloc(8);
@@ -738,7 +746,15 @@ static void launch_fwd(Ctx& c, const T* fv, const T* X, int64_t xstride, const d
   const int N = (int)c.h.N, D = (int)c.h.D;
   DevBands bd = bands_of(c);
   const int RB = rows_per_block(N);
-  if ((rows < 0 ? c.sched.fwd_rows : rows) && RB > 0) {
+  if (std::is_same<T, double>::value && c.mask_option != 0 && c.f_finite && c.xmask.p != nullptr) {
+    // FP64: the column-tiled form visiting only the rows of X where a
+    // warp's column group is non-zero (the same bits)
+    const int M = (int)c.h.M, ng = cdiv(N, 32), nseg = cdiv(M, 32);
+    k_row_masks<T><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), B), 256, 0, c.st>>>(X, xstride, M, N, c.xmask.p);
+    post_launch(c);
+    k_fwd<T, MODE><<<dim3(cdiv(N, kBX), cdiv(D, kBY), B), dim3(kBX, kBY), 0, c.st>>>(bd, fv, X, xstride, P, R, nullptr,
+                                                                                    pred, c.xmask.p);
+  } else if ((rows < 0 ? c.sched.fwd_rows : rows) && RB > 0) {
     const int threads = cdiv((int64_t)RB * N, 32) * 32;
     k_fwd_rows<T, MODE><<<dim3(cdiv(D, RB), B), threads, 0, c.st>>>(bd, fv, X, xstride, P, R, RB, pred);
   } else {
@@ -3278,6 +3294,10 @@ int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
     } else if (n == "tc_persistent") {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "tc_persistent must be -1, 0 or 1");
       c->tc_persistent_option = (int)value;
+    } else if (n == "row_masks") {
+      if (value < 0 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "row_masks must be 0 or 1");
+      c->mask_option = (int)value;
+      c->drop_graphs();  // captured CG chunks hold the products' form
     } else if (n == "tc_screen") {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "tc_screen must be -1, 0 or 1");
       c->tc_screen_option = (int)value;
@@ -3335,6 +3355,7 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     else if (n == "rows_kernels") *value = c->rows_option;
     else if (n == "tc_persistent") *value = c->tc_persistent_option;
     else if (n == "tc_screen") *value = c->tc_screen_option;
+    else if (n == "row_masks") *value = c->mask_option;
     else if (n == "tensor_cores") *value = c->tc_option;
     else if (n == "df_products") *value = c->df_option;
     else if (n == "df_rows") *value = c->df_rows;

@@ -213,18 +213,45 @@ def test_option_errors(built):
 @pytest.mark.parametrize("rows", [1, 0])
 def test_row_flattened_products_bitwise(built, mid, rows):
     """The row-flattened FP64 products (every lane busy for N = 40) give the
-    oracle's trajectory bit for bit, as the column-tiled ones do."""
+    oracle's trajectory bit for bit, as the column-tiled ones do (the
+    forward product's row-occupancy masks off, so each form runs)."""
     import pqdts_gb300 as pq
     from oracle.oracle import Oracle
 
     with pq.Solver(0) as s:
         s.set_option("rows_kernels", rows)
+        s.set_option("row_masks", 0)
         s.set_instance(mid)
         assert s.get_option("sched.fwd_rows") == rows and s.get_option("sched.trans_rows") == rows
         st = s.solve(mode=2, maxiter=200, eps=mid.eps)
         X = s.get_x()
     Xo, so = Oracle.from_instance(mid).solve(mode=2, maxiter=200, eps=mid.eps)
     assert st["L"] == so["L"] and st["cg"] == so["cg"] and np.array_equal(X, Xo)
+
+
+@pytest.mark.parametrize("which", ["cfg1", "mid", "small"])
+def test_row_masks_bitwise(built, request, which):
+    """The FP64 forward products with row-occupancy masks (each warp visits
+    only the rows of X where its 32 columns hold a non-zero) give the same
+    bits as the full chains: the whole trajectory with masks on and off, and
+    the oracle's."""
+    import pqdts_gb300 as pq
+    from oracle.oracle import Oracle
+
+    inst = request.getfixturevalue(which)
+    out = []
+    for masks in (1, 0):
+        with pq.Solver(0) as s:
+            s.set_option("row_masks", masks)
+            s.set_instance(inst)
+            assert s.get_option("row_masks") == masks
+            st = s.solve(mode=2, maxiter=200, eps=inst.eps)
+            out.append((st, s.get_x()))
+    (s1, X1), (s0, X0) = out
+    assert s1["L"] == s0["L"] and s1["cg"] == s0["cg"] and np.array_equal(X1, X0)
+    Xo, so = Oracle.from_instance(inst).solve(mode=2, maxiter=200, eps=inst.eps)
+    assert s1["L"] == so["L"] and np.array_equal(X1, Xo)
+    assert np.mean(X1 == 0.0) > 0.3  # the masks had zeros to skip
 
 
 @pytest.mark.parametrize("shape", [(2, 1, 3), (3, 2, 1), (5, 33, 4), (40, 3, 2)])
