@@ -536,15 +536,15 @@ static int df_rows_per_block(int64_t rows, int N, int rbopt, int sms) {
 }
 
 template <int MODE>
-static void launch_fwd_df(Ctx& c, double* R) {
+static void launch_fwd_df(Ctx& c, double* R, const uint32_t* xmask) {
   const int N = (int)c.h.N, D = (int)c.h.D;
   const int rb = df_rows_per_block(D, N, c.df_rows, c.num_sms);
   const dim3 grid(cdiv(D, rb), cdiv(N, 32 * kDfColWarps));
   const int threads = 32 * std::min(kDfColWarps, cdiv(N, 32));
   DevBands bd = bands_of(c);
-  if (rb == 8) k_fwd_df<MODE, 8><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R);
-  else if (rb == 4) k_fwd_df<MODE, 4><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R);
-  else k_fwd_df<MODE, 2><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R);
+  if (rb == 8) k_fwd_df<MODE, 8><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R, xmask);
+  else if (rb == 4) k_fwd_df<MODE, 4><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R, xmask);
+  else k_fwd_df<MODE, 2><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R, xmask);
   post_launch(c);
 }
 
@@ -773,7 +773,16 @@ static void fwd_df(Ctx& c, const double* X, double* R) {
   require(c.xdf.p, "xdf");
   k_split_df<<<elem_grid(MN), 256, 0, c.st>>>(X, MN, 1.0, c.xdf.p);
   post_launch(c);
-  launch_fwd_df<MODE>(c, R);
+  const uint32_t* xm = nullptr;
+  if (c.mask_option != 0 && c.f_finite) {
+    // X's row-occupancy masks: the product visits only rows where a warp's
+    // columns are non-zero
+    const int M = (int)c.h.M, ng = cdiv(c.h.N, 32), nseg = cdiv(M, 32);
+    k_row_masks<double><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), 1), 256, 0, c.st>>>(X, 0, M, (int)c.h.N, c.xmask.p);
+    post_launch(c);
+    xm = c.xmask.p;
+  }
+  launch_fwd_df<MODE>(c, R, xm);
 }
 
 static void objective_stack(Ctx& c, const double* Xs, int B) {

@@ -271,3 +271,50 @@ def test_L_dL_double_float(built, request, which, full):
     err = np.max(np.abs(G - Go)) / np.max(np.abs(Go))
     assert err < 1e-11, err
     s.close()
+
+
+def _sparse_x(inst, seed):
+    """A feasible X that is zero except near n = 0.6 i N / M and in the last
+    column: the shape of a tomography iterate (an outcome reached from photon
+    numbers near n / eta, the tail mass in the last column)."""
+    rng = np.random.default_rng(seed)
+    M, N = inst.M, inst.N
+    X = np.zeros((M, N))
+    for i in range(M):
+        c = min(N - 1, int(0.6 * i * N / M))
+        lo, hi = max(0, c - 2), min(N, c + 3)
+        X[i, lo:hi] = rng.random(hi - lo)
+        X[i, N - 1] = rng.random()
+    return np.asfortranarray(X / X.sum(1, keepdims=True))
+
+
+@pytest.mark.parametrize("which", ["cfg1", "wide", "banded"])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_row_masks_forward_product(built, request, which, precision):
+    """The forward product visiting only the rows of X where a warp's 32
+    columns hold a non-zero (row-occupancy masks): FP64 -- the same bits as
+    the full chains; double-FP32 (mixed) -- the same objective to 1e-14 and
+    the oracle's to 1e-12."""
+    import pqdts_gb300 as pq
+    from oracle.oracle import Oracle
+    from pqdts_gb300 import synth
+
+    if which == "banded":
+        inst = synth.make_instance(M=300, N=200, D=600, xmax=250.0, eta=0.8, shots=10**6, gamma=1e-4, eps=1e-6, seed=8)
+    else:
+        inst = _df_instances()[which] if which == "wide" else request.getfixturevalue(which)
+    X = _sparse_x(inst, 5)
+    assert np.mean(X == 0.0) > 0.5
+    out = {}
+    for masks in (1, 0):
+        with pq.Solver(0) as s:
+            s.set_option("row_masks", masks)
+            s.set_instance(inst, precision)
+            s.set_x(X)
+            out[masks] = s.L()
+    Lo, _ = Oracle.from_instance(inst).L(X)
+    if precision == 0:
+        assert out[1] == out[0] == Lo
+    else:
+        assert abs(out[1] - out[0]) <= 1e-14 * abs(out[0])
+        assert abs(out[1] - Lo) <= 1e-12 * abs(Lo)
