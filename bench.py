@@ -477,9 +477,10 @@ def run_ours(args):
     # the region timers (CUDA events, ~4 us per span inside a captured CG
     # graph) are read from one solve; the warm-up and timed solves run
     # without them
-    bf0 = s.timer("BF")
+    s.set_option("timers", 2)  # with the spans of the Hessian product's two products
+    bf0, fw0, tr0 = s.timer("BF"), s.timer("BF.fwd"), s.timer("BF.trans")
     _, st_t = timed_solves(s, 1, eps_run, tgt)
-    bf1 = s.timer("BF")
+    bf1, fw1, tr1 = s.timer("BF"), s.timer("BF.fwd"), s.timer("BF.trans")
     s.set_option("timers", 0)
     timed_solves(s, args.warmup, eps_run, tgt)
     launches0 = s.kernel_launches()
@@ -503,13 +504,18 @@ def run_ours(args):
     replicas = replica_check(dist, stats[-1], dev)
     assert replicas["identical"], f"ranks did different work on the same instance: {replicas}"
 
-    # roofline of the dominant kernels: the banded products of the CG's
-    # Hessian product (k_fwd + k_trans), FP64- (or FP32-) ALU bound.
+    # roofline of the dominant kernel: the transposed product of the CG's
+    # Hessian product (k_trans: F^T.(2 F.V) with the stencil, projection,
+    # mask and p.Hp epilogue), FP64-ALU bound; its forward product (k_fwd
+    # with row-occupancy masks) is reported beside it
     nnz, N, M, D = inst.nnz, inst.N, inst.M, inst.D
     cg = st_t[0]["cg"]  # the CG iterations of the solve whose regions were timed
     bf_time = bf1[0] - bf0[0]
+    tr_time, tr_n = tr1[0] - tr0[0], tr1[1] - tr0[1]
+    fw_time, fw_n = fw1[0] - fw0[0], fw1[1] - fw0[1]
     flops_pair = 2 * 2.0 * nnz * N
-    achieved_tf = flops_pair * cg / bf_time / 1e12 if bf_time > 0 else None
+    flops_one = flops_pair / 2
+    achieved_tf = flops_one * tr_n / tr_time / 1e12 if tr_time > 0 else None
     peaks = measured_peaks()
     if prec == pq.FP64:
         peak_tf = fp64_peak_tflops(dev)
@@ -520,21 +526,30 @@ def run_ours(args):
     sval = 8 if prec == pq.FP64 else 4
     bytes_pass = nnz * (sval + 4) + (D + 1) * 8 + M * N * sval + D * N * sval
     traffic = profile_traffic("spmm_fp64_config2.txt" if prec == pq.FP64 else "spmm_fp32_config2.txt")
+    hbm_gbs = bytes_pass * tr_n / tr_time / 1e9 if tr_time > 0 else None
     roofline = {
-        "kernel": "k_fwd + k_trans (Hessian product: O = F.V, F^T.(2O) + stencil)",
-        "timed": "GPU events around the CG's Hessian products in one solve of the workload (region timers on)",
+        "kernel": "k_trans (the Hessian product's F^T.(2 F.V) + stencil, projection, active-set mask, p.Hp)",
+        "timed": "GPU events around each of the CG's transposed products in one solve of the workload "
+                 "(region timers on)",
         "bound": "fp64" if prec == pq.FP64 else "fp32",
         "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
         "frac": (achieved_tf / peak_tf) if (achieved_tf and peak_tf) else None,
         "peak_source": peak_note,
         "traffic": traffic,
-        "algorithmic_flops_per_launch": flops_pair / 2,
+        "algorithmic_flops_per_launch": flops_one,
         "algorithmic_bytes_per_launch": bytes_pass,
-        "hbm_view": {"achieved": bytes_pass * 2 * cg / bf_time / 1e9 if bf_time > 0 else None,
-                     "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-                     "frac": (bytes_pass * 2 * cg / bf_time / 1e9 / peaks["hbm_gbs"]) if (bf_time > 0 and
-                                                                                        peaks.get("hbm_gbs")) else None,
+        "us_per_launch": tr_time / tr_n * 1e6 if tr_n else None,
+        "hbm_view": {"achieved": hbm_gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": (hbm_gbs / peaks["hbm_gbs"]) if (hbm_gbs and peaks.get("hbm_gbs")) else None,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+        "forward_product": {
+            "kernel": "k_fwd with row-occupancy masks (F.V visiting only the rows where a warp's 32 columns of V "
+                      "are non-zero; the same bits as the full chain)",
+            "us_per_launch": fw_time / fw_n * 1e6 if fw_n else None,
+            "dense_equivalent_tflops": flops_one * fw_n / fw_time / 1e12 if fw_time > 0 else None,
+            "note": "dense-equivalent flops over the time: above the FP64 peak because the skipped terms are exact "
+                    "zeros (the iterate and the CG direction are ~90 % zeros on this workload)"},
+        "hessian_pair_us": bf_time / max(1, cg) * 1e6,
     }
 
     # e2e through the C ABI with host buffers

@@ -1002,7 +1002,11 @@ static void hvp(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, const int8_t* ik
                 const double* pred = nullptr) {
   const int M = (int)c.h.M;
   const T* src = c.fullspace ? b.p.p : b.V.p;
-  launch_fwd<T, 1>(c, fv, src, 0, nullptr, b.R2.p, 1, pred);
+  {
+    Scope sf(c.timers, "BF.fwd", true);
+    launch_fwd<T, 1>(c, fv, src, 0, nullptr, b.R2.p, 1, pred);
+  }
+  Scope st(c.timers, "BF.trans", true);
   launch_trans<T, true>(c, tv, b.R2.p, b.p.p, c.fullspace ? nullptr : b.rs.p, c.fullspace ? 0 : 1,
                         (T)(2.0 * c.h.gam), ik, b.Hp.p, with_dot ? b.p.p : nullptr, with_dot ? c.part.p : nullptr,
                         pred);
