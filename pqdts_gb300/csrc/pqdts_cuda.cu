@@ -356,7 +356,7 @@ struct pqdts_ctx {
   // row-occupancy masks of the FP64 forward products' operand (k_row_masks,
   // up to kBatchLS stacked inputs) and whether they are used: on unless the
   // option row_masks is 0 or F holds a value that is not finite
-  pqdts::DBuf<uint32_t> xmask;
+  pqdts::DBuf<uint32_t> xmask, rmask;
   int mask_option = 1;
   bool f_finite = true;
   int df_option = -1;
@@ -627,6 +627,7 @@ static void setup_device(Ctx& c) {
   c.sqd.alloc(M);
   c.f_finite = std::all_of(h.fval.begin(), h.fval.end(), [](double v) { return std::isfinite(v); });
   c.xmask.alloc((size_t)kBatchLS * cdiv(N, 32) * cdiv(M, 32));
+  c.rmask.alloc((size_t)cdiv(N, 32) * cdiv(D, 32));
   CK(cudaFuncSetAttribute(k_condat_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCondatSmemMax));
   CK(cudaFuncSetAttribute(k_simplex_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCondatSmemMax));
   c.counters.alloc(8);
@@ -881,7 +882,16 @@ static void launch_trans_shape(Ctx& c, TransShape sh, const T* tv, const T* R, c
   const int M = (int)c.h.M;
   DevBands bd = bands_of(c);
   const int RB = rows_per_block((int)c.h.N);
-  if (sh.rows && W == nullptr && c.t_contiguous && RB > 0) {
+  const uint32_t* rmask = nullptr;
+  if (std::is_same<T, double>::value && c.mask_option != 0 && c.f_finite && c.t_contiguous && c.rmask.p != nullptr) {
+    // FP64: the CSR form visiting only the d where a warp's column groups of
+    // R are non-zero (the same bits)
+    const int N = (int)c.h.N, D = (int)c.h.D, ng = cdiv(N, 32), nseg = cdiv(D, 32);
+    k_row_masks<T><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), 1), 256, 0, c.st>>>(R, 0, D, N, c.rmask.p);
+    post_launch(c);
+    rmask = c.rmask.p;
+  }
+  if (sh.rows && W == nullptr && c.t_contiguous && RB > 0 && rmask == nullptr) {
     const int threads = cdiv((int64_t)RB * c.h.N, 32) * 32;
     k_trans_rows<T, HVP><<<cdiv(M, RB), threads, 0, c.st>>>(bd, tv, RB, R, V, rs, c.maxr.p, reduced, c2gam, ik, G,
                                                             pred, Gf);
@@ -890,16 +900,20 @@ static void launch_trans_shape(Ctx& c, TransShape sh, const T* tv, const T* R, c
   }
   switch (sh.C) {
     case 1:
-      k_trans<T, HVP, 1><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf);
+      k_trans<T, HVP, 1><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf,
+                                                      rmask);
       break;
     case 2:
-      k_trans<T, HVP, 2><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf);
+      k_trans<T, HVP, 2><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf,
+                                                      rmask);
       break;
     case 4:
-      k_trans<T, HVP, 4><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf);
+      k_trans<T, HVP, 4><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf,
+                                                      rmask);
       break;
     default:
-      k_trans<T, HVP, 8><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf);
+      k_trans<T, HVP, 8><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf,
+                                                      rmask);
       break;
   }
   post_launch(c);
