@@ -291,10 +291,11 @@ def _sparse_x(inst, seed):
 @pytest.mark.parametrize("which", ["cfg1", "wide", "banded"])
 @pytest.mark.parametrize("precision", [0, 1])
 def test_row_masks_forward_product(built, request, which, precision):
-    """The forward product visiting only the rows of X where a warp's 32
-    columns hold a non-zero (row-occupancy masks): FP64 -- the same bits as
-    the full chains; double-FP32 (mixed) -- the same objective to 1e-14 and
-    the oracle's to 1e-12."""
+    """The banded products visiting only the rows of their operand (X for
+    F.X, R for F^T.R) where a warp's 32 columns hold a non-zero (row-occupancy
+    masks): FP64 -- the same bits as the full chains and the oracle's;
+    double-FP32 (mixed) -- the same objective to 1e-14 and gradient to 1e-13
+    of its scale, and the oracle's to 1e-12 / 1e-11."""
     import pqdts_gb300 as pq
     from oracle.oracle import Oracle
     from pqdts_gb300 import synth
@@ -311,10 +312,18 @@ def test_row_masks_forward_product(built, request, which, precision):
             s.set_option("row_masks", masks)
             s.set_instance(inst, precision)
             s.set_x(X)
-            out[masks] = s.L()
-    Lo, _ = Oracle.from_instance(inst).L(X)
+            L = s.L()
+            s.set_x(X)
+            out[masks] = (L, s.dL())
+    o = Oracle.from_instance(inst)
+    Lo, _ = o.L(X)
+    Go, _ = o.dL(X)
+    (L1, G1), (L0, G0) = out[1], out[0]
     if precision == 0:
-        assert out[1] == out[0] == Lo
+        assert L1 == L0 == Lo
+        assert np.array_equal(G1, G0) and np.array_equal(G1, Go)
     else:
-        assert abs(out[1] - out[0]) <= 1e-14 * abs(out[0])
-        assert abs(out[1] - Lo) <= 1e-12 * abs(Lo)
+        assert abs(L1 - L0) <= 1e-14 * abs(L0)
+        assert abs(L1 - Lo) <= 1e-12 * abs(Lo)
+        assert np.max(np.abs(G1 - G0)) <= 1e-13 * np.max(np.abs(G0))
+        assert np.max(np.abs(G1 - Go)) <= 1e-11 * np.max(np.abs(Go))
