@@ -356,10 +356,8 @@ struct pqdts_ctx {
   // row-occupancy masks of the FP64 forward products' operand (k_row_masks,
   // up to kBatchLS stacked inputs) and whether they are used: on unless the
   // option row_masks is 0 or F holds a value that is not finite
-  pqdts::DBuf<uint32_t> xmask, rmask;
-  pqdts::DBuf<unsigned> mcount;  // set bits of xmask ([0]) and rmask ([1])
+  pqdts::DBuf<uint32_t> xmask;
   int mask_option = 1;
-  int mask_dense_pct = 50;  // the masked loops run while at most this share of the mask bits is set
   bool f_finite = true;
   int df_option = -1;
   int df_rows = 0;  // band rows per block of the double-FP32 products (0: chosen by size)
@@ -544,11 +542,9 @@ static void launch_fwd_df(Ctx& c, double* R, const uint32_t* xmask) {
   const dim3 grid(cdiv(D, rb), cdiv(N, 32 * kDfColWarps));
   const int threads = 32 * std::min(kDfColWarps, cdiv(N, 32));
   DevBands bd = bands_of(c);
-  const unsigned dense = (unsigned)((int64_t)cdiv(c.h.M, 32) * cdiv(N, 32) * 32 * c.mask_dense_pct / 100);
-  const unsigned* cnt = c.mcount.p;
-  if (rb == 8) k_fwd_df<MODE, 8><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R, xmask, cnt, dense);
-  else if (rb == 4) k_fwd_df<MODE, 4><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R, xmask, cnt, dense);
-  else k_fwd_df<MODE, 2><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R, xmask, cnt, dense);
+  if (rb == 8) k_fwd_df<MODE, 8><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R, xmask);
+  else if (rb == 4) k_fwd_df<MODE, 4><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R, xmask);
+  else k_fwd_df<MODE, 2><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R, xmask);
   post_launch(c);
 }
 
@@ -631,8 +627,6 @@ static void setup_device(Ctx& c) {
   c.sqd.alloc(M);
   c.f_finite = std::all_of(h.fval.begin(), h.fval.end(), [](double v) { return std::isfinite(v); });
   c.xmask.alloc((size_t)kBatchLS * cdiv(N, 32) * cdiv(M, 32));
-  c.rmask.alloc((size_t)cdiv(N, 32) * cdiv(D, 32));
-  c.mcount.alloc(2);
   CK(cudaFuncSetAttribute(k_condat_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCondatSmemMax));
   CK(cudaFuncSetAttribute(k_simplex_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCondatSmemMax));
   c.counters.alloc(8);
@@ -756,13 +750,10 @@ static void launch_fwd(Ctx& c, const T* fv, const T* X, int64_t xstride, const d
     // FP64: the column-tiled form visiting only the rows of X where a
     // warp's column group is non-zero (the same bits)
     const int M = (int)c.h.M, ng = cdiv(N, 32), nseg = cdiv(M, 32);
-    CK(cudaMemsetAsync(c.mcount.p, 0, sizeof(unsigned), c.st));
-    k_row_masks<T><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), B), 256, 0, c.st>>>(X, xstride, M, N, c.xmask.p,
-                                                                                 c.mcount.p);
+    k_row_masks<T><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), B), 256, 0, c.st>>>(X, xstride, M, N, c.xmask.p);
     post_launch(c);
-    const unsigned dense = (unsigned)((int64_t)B * nseg * ng * 32 * c.mask_dense_pct / 100);
     k_fwd<T, MODE><<<dim3(cdiv(N, kBX), cdiv(D, kBY), B), dim3(kBX, kBY), 0, c.st>>>(bd, fv, X, xstride, P, R, nullptr,
-                                                                                    pred, c.xmask.p, c.mcount.p, dense);
+                                                                                    pred, c.xmask.p);
   } else if ((rows < 0 ? c.sched.fwd_rows : rows) && RB > 0) {
     const int threads = cdiv((int64_t)RB * N, 32) * 32;
     k_fwd_rows<T, MODE><<<dim3(cdiv(D, RB), B), threads, 0, c.st>>>(bd, fv, X, xstride, P, R, RB, pred);
@@ -787,9 +778,7 @@ static void fwd_df(Ctx& c, const double* X, double* R) {
     // X's row-occupancy masks: the product visits only rows where a warp's
     // columns are non-zero
     const int M = (int)c.h.M, ng = cdiv(c.h.N, 32), nseg = cdiv(M, 32);
-    CK(cudaMemsetAsync(c.mcount.p, 0, sizeof(unsigned), c.st));
-    k_row_masks<double><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), 1), 256, 0, c.st>>>(X, 0, M, (int)c.h.N, c.xmask.p,
-                                                                                      c.mcount.p);
+    k_row_masks<double><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), 1), 256, 0, c.st>>>(X, 0, M, (int)c.h.N, c.xmask.p);
     post_launch(c);
     xm = c.xmask.p;
   }
@@ -892,20 +881,7 @@ static void launch_trans_shape(Ctx& c, TransShape sh, const T* tv, const T* R, c
   const int M = (int)c.h.M;
   DevBands bd = bands_of(c);
   const int RB = rows_per_block((int)c.h.N);
-  const uint32_t* rmask = nullptr;
-  unsigned rdense = 0u;
-  if (std::is_same<T, double>::value && c.mask_option != 0 && c.f_finite && c.t_contiguous && c.rmask.p != nullptr) {
-    // FP64: the CSR form visiting only the d where a warp's column groups of
-    // R are non-zero (the same bits)
-    const int N = (int)c.h.N, D = (int)c.h.D, ng = cdiv(N, 32), nseg = cdiv(D, 32);
-    CK(cudaMemsetAsync(c.mcount.p + 1, 0, sizeof(unsigned), c.st));
-    k_row_masks<T><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), 1), 256, 0, c.st>>>(R, 0, D, N, c.rmask.p,
-                                                                                 c.mcount.p + 1);
-    post_launch(c);
-    rmask = c.rmask.p;
-    rdense = (unsigned)((int64_t)nseg * ng * 32 * c.mask_dense_pct / 100);
-  }
-  if (sh.rows && W == nullptr && c.t_contiguous && RB > 0 && rmask == nullptr) {
+  if (sh.rows && W == nullptr && c.t_contiguous && RB > 0) {
     const int threads = cdiv((int64_t)RB * c.h.N, 32) * 32;
     k_trans_rows<T, HVP><<<cdiv(M, RB), threads, 0, c.st>>>(bd, tv, RB, R, V, rs, c.maxr.p, reduced, c2gam, ik, G,
                                                             pred, Gf);
@@ -914,20 +890,16 @@ static void launch_trans_shape(Ctx& c, TransShape sh, const T* tv, const T* R, c
   }
   switch (sh.C) {
     case 1:
-      k_trans<T, HVP, 1><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf,
-                                                      rmask, c.mcount.p + 1, rdense);
+      k_trans<T, HVP, 1><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf);
       break;
     case 2:
-      k_trans<T, HVP, 2><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf,
-                                                      rmask, c.mcount.p + 1, rdense);
+      k_trans<T, HVP, 2><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf);
       break;
     case 4:
-      k_trans<T, HVP, 4><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf,
-                                                      rmask, c.mcount.p + 1, rdense);
+      k_trans<T, HVP, 4><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf);
       break;
     default:
-      k_trans<T, HVP, 8><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf,
-                                                      rmask, c.mcount.p + 1, rdense);
+      k_trans<T, HVP, 8><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf);
       break;
   }
   post_launch(c);
@@ -965,30 +937,15 @@ static void op_dL(Ctx& c) {
     const int D = (int)c.h.D;
     k_split_df<<<elem_grid((int64_t)D * N), 256, 0, c.st>>>(c.R.p, (int64_t)D * N, 1.0, c.rdf.p);
     post_launch(c);
-    // R's row-occupancy masks: the product visits only the d where a warp's
-    // columns of R are non-zero
-    const uint32_t* rm = nullptr;
-    unsigned rdense = 0u;
-    if (c.mask_option != 0 && c.f_finite) {
-      const int ng = cdiv(N, 32), nseg = cdiv(D, 32);
-      CK(cudaMemsetAsync(c.mcount.p + 1, 0, sizeof(unsigned), c.st));
-      k_row_masks<double><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), 1), 256, 0, c.st>>>(c.R.p, 0, D, N, c.rmask.p,
-                                                                                        c.mcount.p + 1);
-      post_launch(c);
-      rm = c.rmask.p;
-      rdense = (unsigned)((int64_t)nseg * ng * 32 * c.mask_dense_pct / 100);
-    }
     double* g = c.fullspace ? c.G.p : nullptr;
     const double c2g = 2.0 * c.h.gam;
     const int rb = df_rows_per_block(M, N, c.df_rows, c.num_sms);
     const dim3 grid(cdiv(M, rb), cdiv(N, 32 * kDfColWarps));
     const int threads = 32 * std::min(kDfColWarps, cdiv(N, 32));
     DevBands bd = bands_of(c);
-    const unsigned* rc = c.mcount.p + 1;
-    if (rb == 8) k_trans_df<8><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p, rm, rc, rdense);
-    else if (rb == 4)
-      k_trans_df<4><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p, rm, rc, rdense);
-    else k_trans_df<2><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p, rm, rc, rdense);
+    if (rb == 8) k_trans_df<8><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
+    else if (rb == 4) k_trans_df<4><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
+    else k_trans_df<2><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
     post_launch(c);
     if (!c.fullspace) {
       k_reduced_from_full<<<M, std::min(256, std::max(32, cdiv(N, 32) * 32)), 0, c.st>>>(c.Gf.p, c.maxr.p, N, c.G.p);
@@ -3354,10 +3311,6 @@ int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
       if (value < 0 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "row_masks must be 0 or 1");
       c->mask_option = (int)value;
       c->drop_graphs();  // captured CG chunks hold the products' form
-    } else if (n == "row_masks_dense_pct") {
-      if (value < 0 || value > 100) throw pqdts::Err(PQDTS_E_ARG, "row_masks_dense_pct must be 0..100");
-      c->mask_dense_pct = (int)value;
-      c->drop_graphs();
     } else if (n == "tc_screen") {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "tc_screen must be -1, 0 or 1");
       c->tc_screen_option = (int)value;
@@ -3416,7 +3369,6 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     else if (n == "tc_persistent") *value = c->tc_persistent_option;
     else if (n == "tc_screen") *value = c->tc_screen_option;
     else if (n == "row_masks") *value = c->mask_option;
-    else if (n == "row_masks_dense_pct") *value = c->mask_dense_pct;
     else if (n == "tensor_cores") *value = c->tc_option;
     else if (n == "df_products") *value = c->df_option;
     else if (n == "df_rows") *value = c->df_rows;

@@ -291,11 +291,11 @@ def _sparse_x(inst, seed):
 @pytest.mark.parametrize("which", ["cfg1", "wide", "banded"])
 @pytest.mark.parametrize("precision", [0, 1])
 def test_row_masks_forward_product(built, request, which, precision):
-    """The banded products visiting only the rows of their operand (X for
-    F.X, R for F^T.R) where a warp's 32 columns hold a non-zero (row-occupancy
-    masks): FP64 -- the same bits as the full chains and the oracle's;
-    double-FP32 (mixed) -- the same objective to 1e-14 and gradient to 1e-13
-    of its scale, and the oracle's to 1e-12 / 1e-11."""
+    """The forward product F.X visiting only the rows of X where a warp's 32
+    columns hold a non-zero (row-occupancy masks): FP64 -- the same bits as
+    the full chains, in L and in dL (whose residual it forms), and the
+    oracle's; double-FP32 (mixed) -- the same objective to 1e-14 and
+    gradient to 1e-13 of its scale, and the oracle's to 1e-12 / 1e-11."""
     import pqdts_gb300 as pq
     from oracle.oracle import Oracle
     from pqdts_gb300 import synth
