@@ -356,7 +356,7 @@ struct pqdts_ctx {
   // row-occupancy masks of the FP64 forward products' operand (k_row_masks,
   // up to kBatchLS stacked inputs) and whether they are used: on unless the
   // option row_masks is 0 or F holds a value that is not finite
-  pqdts::DBuf<uint32_t> xmask;
+  pqdts::DBuf<uint32_t> xmask, rmask;
   int mask_option = 1;
   bool f_finite = true;
   int df_option = -1;
@@ -539,8 +539,9 @@ template <int MODE>
 static void launch_fwd_df(Ctx& c, double* R, const uint32_t* xmask) {
   const int N = (int)c.h.N, D = (int)c.h.D;
   const int rb = df_rows_per_block(D, N, c.df_rows, c.num_sms);
-  const dim3 grid(cdiv(D, rb), cdiv(N, 32 * kDfColWarps));
-  const int threads = 32 * std::min(kDfColWarps, cdiv(N, 32));
+  // with masks one column group per block (a sparse group's block ends early)
+  const int threads = xmask ? 32 : 32 * std::min(kDfColWarps, cdiv(N, 32));
+  const dim3 grid(cdiv(D, rb), cdiv(N, threads));
   DevBands bd = bands_of(c);
   if (rb == 8) k_fwd_df<MODE, 8><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R, xmask);
   else if (rb == 4) k_fwd_df<MODE, 4><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R, xmask);
@@ -627,6 +628,7 @@ static void setup_device(Ctx& c) {
   c.sqd.alloc(M);
   c.f_finite = std::all_of(h.fval.begin(), h.fval.end(), [](double v) { return std::isfinite(v); });
   c.xmask.alloc((size_t)kBatchLS * cdiv(N, 32) * cdiv(M, 32));
+  c.rmask.alloc((size_t)cdiv(N, 32) * cdiv(D, 32));
   CK(cudaFuncSetAttribute(k_condat_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCondatSmemMax));
   CK(cudaFuncSetAttribute(k_simplex_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCondatSmemMax));
   c.counters.alloc(8);
@@ -881,7 +883,18 @@ static void launch_trans_shape(Ctx& c, TransShape sh, const T* tv, const T* R, c
   const int M = (int)c.h.M;
   DevBands bd = bands_of(c);
   const int RB = rows_per_block((int)c.h.N);
-  if (sh.rows && W == nullptr && c.t_contiguous && RB > 0) {
+  int raw = 0;
+  if (std::is_same<T, double>::value && c.mask_option != 0 && c.f_finite && c.t_contiguous && c.rmask.p != nullptr) {
+    // FP64: the sums by (row, column group) warps visiting only the d where
+    // the group's columns of R are non-zero (R's row-occupancy masks; the
+    // same bits), then k_trans's epilogue on them
+    const int N = (int)c.h.N, D = (int)c.h.D, ng = cdiv(N, 32), nseg = cdiv(D, 32);
+    k_row_masks<T><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), 1), 256, 0, c.st>>>(R, 0, D, N, c.rmask.p);
+    post_launch(c);
+    k_trans_grp<T><<<dim3(M, ng), 32, 0, c.st>>>(bd, tv, R, c.rmask.p, G, pred);
+    post_launch(c);
+    raw = 1;
+  } else if (sh.rows && W == nullptr && c.t_contiguous && RB > 0) {
     const int threads = cdiv((int64_t)RB * c.h.N, 32) * 32;
     k_trans_rows<T, HVP><<<cdiv(M, RB), threads, 0, c.st>>>(bd, tv, RB, R, V, rs, c.maxr.p, reduced, c2gam, ik, G,
                                                             pred, Gf);
@@ -890,16 +903,20 @@ static void launch_trans_shape(Ctx& c, TransShape sh, const T* tv, const T* R, c
   }
   switch (sh.C) {
     case 1:
-      k_trans<T, HVP, 1><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf);
+      k_trans<T, HVP, 1><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf,
+                                                      raw);
       break;
     case 2:
-      k_trans<T, HVP, 2><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf);
+      k_trans<T, HVP, 2><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf,
+                                                      raw);
       break;
     case 4:
-      k_trans<T, HVP, 4><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf);
+      k_trans<T, HVP, 4><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf,
+                                                      raw);
       break;
     default:
-      k_trans<T, HVP, 8><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf);
+      k_trans<T, HVP, 8><<<M, sh.threads, 0, c.st>>>(bd, tv, R, V, rs, c.maxr.p, reduced, c2gam, ik, G, W, dpart, pred, Gf,
+                                                      raw);
       break;
   }
   post_launch(c);
@@ -937,15 +954,24 @@ static void op_dL(Ctx& c) {
     const int D = (int)c.h.D;
     k_split_df<<<elem_grid((int64_t)D * N), 256, 0, c.st>>>(c.R.p, (int64_t)D * N, 1.0, c.rdf.p);
     post_launch(c);
+    // R's row-occupancy masks: each block (one column group) visits only the
+    // d where its columns of R are non-zero
+    const uint32_t* rm = nullptr;
+    if (c.mask_option != 0 && c.f_finite) {
+      const int ng = cdiv(N, 32), nseg = cdiv(D, 32);
+      k_row_masks<double><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), 1), 256, 0, c.st>>>(c.R.p, 0, D, N, c.rmask.p);
+      post_launch(c);
+      rm = c.rmask.p;
+    }
     double* g = c.fullspace ? c.G.p : nullptr;
     const double c2g = 2.0 * c.h.gam;
     const int rb = df_rows_per_block(M, N, c.df_rows, c.num_sms);
-    const dim3 grid(cdiv(M, rb), cdiv(N, 32 * kDfColWarps));
-    const int threads = 32 * std::min(kDfColWarps, cdiv(N, 32));
+    const int threads = rm ? 32 : 32 * std::min(kDfColWarps, cdiv(N, 32));
+    const dim3 grid(cdiv(M, rb), cdiv(N, threads));
     DevBands bd = bands_of(c);
-    if (rb == 8) k_trans_df<8><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
-    else if (rb == 4) k_trans_df<4><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
-    else k_trans_df<2><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
+    if (rb == 8) k_trans_df<8><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p, rm);
+    else if (rb == 4) k_trans_df<4><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p, rm);
+    else k_trans_df<2><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p, rm);
     post_launch(c);
     if (!c.fullspace) {
       k_reduced_from_full<<<M, std::min(256, std::max(32, cdiv(N, 32) * 32)), 0, c.st>>>(c.Gf.p, c.maxr.p, N, c.G.p);
