@@ -678,6 +678,11 @@ def run_profile_case(case):
         3x L at a random feasible X -- real banded-product launches only
         (fp64: row-flattened products, no autotuning launches);
       solve64 / solvemix: one full benchmark solve (the launch list);
+      fp64sp: the FP64 Hessian product (3x BF), 3x dL and 3x L at the
+        FP64 solution of the workload (a sparse Pi, as the solve's iterates
+        are once in stage 2: the row-occupancy masks of the products see
+        the zeros they skip in the solve); V = that Pi minus 1/N on its
+        non-zeros, so it has the same zeros;
       solvemix3: the mixed solve of M=10000 N=1000 D=20000 to its own
         stopping rule conv < 1e-6 (no FP64 solve first: the launch list of
         the mixed solver alone)."""
@@ -722,6 +727,24 @@ def run_profile_case(case):
             s.set_option("autotune", 0)
             s.set_option("rows_kernels", 1)
         s.set_instance(inst, prec)
+        if case == "fp64sp":
+            with pq.Solver(0) as s64:
+                s64.set_instance(inst, pq.FP64)
+                s64.solve(mode=2, maxiter=MAXITER, eps=EPS)
+                Xs = s64.get_x()
+            s.set_option("autotune", 0)
+            V = np.where(Xs != 0.0, Xs - 1.0 / inst.N, 0.0)
+            for _ in range(3):
+                s.BF(np.asfortranarray(V))
+            for _ in range(3):
+                s.set_x(Xs)
+                s.dL()
+            for _ in range(3):
+                s.set_x(Xs)
+                s.L()
+            print(json.dumps({"profile_case": case, "zero_frac": float(np.mean(Xs == 0.0)),
+                              "launches": s.kernel_launches()}))
+            return 0
         if case.startswith("solve"):
             L64 = None
             if prec == pq.MIXED:
@@ -848,8 +871,8 @@ def main():
     ap.add_argument("--no-mixed", dest="with_mixed", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-sample-iters", type=int, default=3)
-    ap.add_argument("--profile-case", choices=["fp64", "mixed", "solve64", "solvemix", "solvemix3", "tc3", "tcdense",
-                                               "tc3p", "tcdensep"], default=None,
+    ap.add_argument("--profile-case", choices=["fp64", "fp64sp", "mixed", "solve64", "solvemix", "solvemix3", "tc3",
+                                               "tcdense", "tc3p", "tcdensep"], default=None,
                     help="launches of the workload for ncu (see run_profile_case)")
     ap.add_argument("--workload", choices=["batch", "config3", "dense", "config5"], default=None,
                     help="secondary measurement instead of the bench line")
