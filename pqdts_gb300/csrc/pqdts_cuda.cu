@@ -539,8 +539,7 @@ template <int MODE>
 static void launch_fwd_df(Ctx& c, double* R, const uint32_t* xmask) {
   const int N = (int)c.h.N, D = (int)c.h.D;
   const int rb = df_rows_per_block(D, N, c.df_rows, c.num_sms);
-  // with masks one column group per block (a sparse group's block ends early)
-  const int threads = xmask ? 32 : 32 * std::min(kDfColWarps, cdiv(N, 32));
+  const int threads = 32 * std::min(kDfColWarps, cdiv(N, 32));
   const dim3 grid(cdiv(D, rb), cdiv(N, threads));
   DevBands bd = bands_of(c);
   if (rb == 8) k_fwd_df<MODE, 8><<<grid, threads, 0, c.st>>>(bd, c.fdf.p, c.xdf.p, c.P.p, R, xmask);
@@ -954,24 +953,15 @@ static void op_dL(Ctx& c) {
     const int D = (int)c.h.D;
     k_split_df<<<elem_grid((int64_t)D * N), 256, 0, c.st>>>(c.R.p, (int64_t)D * N, 1.0, c.rdf.p);
     post_launch(c);
-    // R's row-occupancy masks: each block (one column group) visits only the
-    // d where its columns of R are non-zero
-    const uint32_t* rm = nullptr;
-    if (c.mask_option != 0 && c.f_finite) {
-      const int ng = cdiv(N, 32), nseg = cdiv(D, 32);
-      k_row_masks<double><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), 1), 256, 0, c.st>>>(c.R.p, 0, D, N, c.rmask.p);
-      post_launch(c);
-      rm = c.rmask.p;
-    }
     double* g = c.fullspace ? c.G.p : nullptr;
     const double c2g = 2.0 * c.h.gam;
     const int rb = df_rows_per_block(M, N, c.df_rows, c.num_sms);
-    const int threads = rm ? 32 : 32 * std::min(kDfColWarps, cdiv(N, 32));
+    const int threads = 32 * std::min(kDfColWarps, cdiv(N, 32));
     const dim3 grid(cdiv(M, rb), cdiv(N, threads));
     DevBands bd = bands_of(c);
-    if (rb == 8) k_trans_df<8><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p, rm);
-    else if (rb == 4) k_trans_df<4><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p, rm);
-    else k_trans_df<2><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p, rm);
+    if (rb == 8) k_trans_df<8><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
+    else if (rb == 4) k_trans_df<4><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
+    else k_trans_df<2><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
     post_launch(c);
     if (!c.fullspace) {
       k_reduced_from_full<<<M, std::min(256, std::max(32, cdiv(N, 32) * 32)), 0, c.st>>>(c.Gf.p, c.maxr.p, N, c.G.p);
