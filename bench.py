@@ -681,8 +681,9 @@ def run_profile_case(case):
       fp64sp: the FP64 Hessian product (3x BF), 3x dL and 3x L at the
         FP64 solution of the workload (a sparse Pi, as the solve's iterates
         are once in stage 2: the row-occupancy masks of the products see
-        the zeros they skip in the solve); V = that Pi minus 1/N on its
-        non-zeros, so it has the same zeros;
+        the zeros they skip in the solve; the solve itself runs without
+        the masks, so the masked kernels' first launches are these); V =
+        that Pi minus 1/N on its non-zeros, so it has the same zeros;
       solvemix3: the mixed solve of M=10000 N=1000 D=20000 to its own
         stopping rule conv < 1e-6 (no FP64 solve first: the launch list of
         the mixed solver alone)."""
@@ -729,6 +730,7 @@ def run_profile_case(case):
         s.set_instance(inst, prec)
         if case == "fp64sp":
             with pq.Solver(0) as s64:
+                s64.set_option("row_masks", 0)  # (no masked-product launches before the profiled ones)
                 s64.set_instance(inst, pq.FP64)
                 s64.solve(mode=2, maxiter=MAXITER, eps=EPS)
                 Xs = s64.get_x()
