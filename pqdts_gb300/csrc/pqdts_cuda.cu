@@ -358,6 +358,10 @@ struct pqdts_ctx {
   // option row_masks is 0 or F holds a value that is not finite
   pqdts::DBuf<uint32_t> xmask, rmask;
   int mask_option = 1;
+  // option count_fmas: the masked FP64 products add the FMAs they execute
+  // (per output lane) to fmacount[0] (forward) and [1] (transposed)
+  bool count_fmas = false;
+  pqdts::DBuf<unsigned long long> fmacount;
   bool f_finite = true;
   int df_option = -1;
   int df_rows = 0;  // band rows per block of the double-FP32 products (0: chosen by size)
@@ -628,6 +632,8 @@ static void setup_device(Ctx& c) {
   c.f_finite = std::all_of(h.fval.begin(), h.fval.end(), [](double v) { return std::isfinite(v); });
   c.xmask.alloc((size_t)kBatchLS * cdiv(N, 32) * cdiv(M, 32));
   c.rmask.alloc((size_t)cdiv(N, 32) * cdiv(D, 32));
+  c.fmacount.alloc(2);
+  CK(cudaMemsetAsync(c.fmacount.p, 0, 2 * sizeof(unsigned long long), c.st));
   CK(cudaFuncSetAttribute(k_condat_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCondatSmemMax));
   CK(cudaFuncSetAttribute(k_simplex_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCondatSmemMax));
   c.counters.alloc(8);
@@ -754,7 +760,8 @@ static void launch_fwd(Ctx& c, const T* fv, const T* X, int64_t xstride, const d
     k_row_masks<T><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), B), 256, 0, c.st>>>(X, xstride, M, N, c.xmask.p);
     post_launch(c);
     k_fwd<T, MODE><<<dim3(cdiv(N, kBX), cdiv(D, kBY), B), dim3(kBX, kBY), 0, c.st>>>(bd, fv, X, xstride, P, R, nullptr,
-                                                                                    pred, c.xmask.p);
+                                                                                    pred, c.xmask.p,
+                                                                                    c.count_fmas ? c.fmacount.p : nullptr);
   } else if ((rows < 0 ? c.sched.fwd_rows : rows) && RB > 0) {
     const int threads = cdiv((int64_t)RB * N, 32) * 32;
     k_fwd_rows<T, MODE><<<dim3(cdiv(D, RB), B), threads, 0, c.st>>>(bd, fv, X, xstride, P, R, RB, pred);
@@ -890,7 +897,8 @@ static void launch_trans_shape(Ctx& c, TransShape sh, const T* tv, const T* R, c
     const int N = (int)c.h.N, D = (int)c.h.D, ng = cdiv(N, 32), nseg = cdiv(D, 32);
     k_row_masks<T><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), 1), 256, 0, c.st>>>(R, 0, D, N, c.rmask.p);
     post_launch(c);
-    k_trans_grp<T><<<dim3(M, ng), 32, 0, c.st>>>(bd, tv, R, c.rmask.p, G, pred);
+    k_trans_grp<T><<<dim3(M, ng), 32, 0, c.st>>>(bd, tv, R, c.rmask.p, G, pred,
+                                                c.count_fmas ? c.fmacount.p + 1 : nullptr);
     post_launch(c);
     raw = 1;
   } else if (sh.rows && W == nullptr && c.t_contiguous && RB > 0) {
@@ -3327,6 +3335,12 @@ int pqdts_cuda_set_option(pqdts_ctx* c, const char* name, int64_t value) {
       if (value < 0 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "row_masks must be 0 or 1");
       c->mask_option = (int)value;
       c->drop_graphs();  // captured CG chunks hold the products' form
+    } else if (n == "count_fmas") {
+      if (value < 0 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "count_fmas must be 0 or 1");
+      c->count_fmas = value != 0;
+      c->drop_graphs();
+    } else if (n == "fmas.forward" || n == "fmas.transposed") {
+      throw pqdts::Err(PQDTS_E_ARG, n + " is read-only");
     } else if (n == "tc_screen") {
       if (value < -1 || value > 1) throw pqdts::Err(PQDTS_E_ARG, "tc_screen must be -1, 0 or 1");
       c->tc_screen_option = (int)value;
@@ -3385,6 +3399,15 @@ int pqdts_cuda_get_option(pqdts_ctx* c, const char* name, int64_t* value) {
     else if (n == "tc_persistent") *value = c->tc_persistent_option;
     else if (n == "tc_screen") *value = c->tc_screen_option;
     else if (n == "row_masks") *value = c->mask_option;
+    else if (n == "count_fmas") *value = c->count_fmas ? 1 : 0;
+    else if (n == "fmas.forward" || n == "fmas.transposed") {
+      unsigned long long v[2] = {0, 0};
+      if (c->fmacount.p) {
+        CK(cudaMemcpyAsync(v, c->fmacount.p, sizeof(v), cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+      }
+      *value = (int64_t)(n == "fmas.forward" ? v[0] : v[1]);
+    }
     else if (n == "tensor_cores") *value = c->tc_option;
     else if (n == "df_products") *value = c->df_option;
     else if (n == "df_rows") *value = c->df_rows;
