@@ -327,3 +327,30 @@ def test_row_masks_forward_product(built, request, which, precision):
         assert abs(L1 - Lo) <= 1e-12 * abs(Lo)
         assert np.max(np.abs(G1 - G0)) <= 1e-13 * np.max(np.abs(G0))
         assert np.max(np.abs(G1 - Go)) <= 1e-11 * np.max(np.abs(Go))
+
+
+def test_row_masks_fma_counts(built, mid):
+    """The masked FP64 products count the FMAs they execute (option
+    count_fmas): with a direction of no zeros every band term runs (nnz * N
+    in each product, as the full chains); with Pi-like zeros fewer, and the
+    Hessian product is the same bits."""
+    import pqdts_gb300 as pq
+
+    inst = mid
+    nnz_n = int(inst.nnz) * inst.N
+    rng = np.random.default_rng(4)
+    dense = np.asfortranarray(rng.standard_normal((inst.M, inst.N)) + 3.0)  # no zeros
+    sparse = _sparse_x(inst, 6)
+    with pq.Solver(0) as s:
+        s.set_instance(inst, pq.FP64)
+        s.set_option("count_fmas", 1)
+        counts = []
+        for V in (dense, sparse):
+            f0, t0 = s.get_option("fmas.forward"), s.get_option("fmas.transposed")
+            H = s.BF(V)
+            counts.append((s.get_option("fmas.forward") - f0, s.get_option("fmas.transposed") - t0))
+        s.set_option("row_masks", 0)
+        H0 = s.BF(sparse)
+    assert counts[0] == (nnz_n, nnz_n), (counts, nnz_n)
+    assert 0 < counts[1][0] < nnz_n and 0 < counts[1][1] <= nnz_n, counts
+    assert np.array_equal(H, H0)
