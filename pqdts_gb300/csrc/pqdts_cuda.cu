@@ -897,7 +897,7 @@ static void launch_trans_shape(Ctx& c, TransShape sh, const T* tv, const T* R, c
     const int N = (int)c.h.N, D = (int)c.h.D, ng = cdiv(N, 32), nseg = cdiv(D, 32);
     k_row_masks<T><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), 1), 256, 0, c.st>>>(R, 0, D, N, c.rmask.p);
     post_launch(c);
-    k_trans_grp<T><<<dim3(M, ng), 32, 0, c.st>>>(bd, tv, R, c.rmask.p, G, pred,
+    k_trans_grp<T><<<dim3(cdiv(M, kTgRows), ng), dim3(32, kTgRows), 0, c.st>>>(bd, tv, R, c.rmask.p, G, pred,
                                                 c.count_fmas ? c.fmacount.p + 1 : nullptr);
     post_launch(c);
     raw = 1;
