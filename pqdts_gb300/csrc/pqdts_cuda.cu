@@ -964,24 +964,12 @@ static void op_dL(Ctx& c) {
     double* g = c.fullspace ? c.G.p : nullptr;
     const double c2g = 2.0 * c.h.gam;
     const int rb = df_rows_per_block(M, N, c.df_rows, c.num_sms);
+    const int threads = 32 * std::min(kDfColWarps, cdiv(N, 32));
+    const dim3 grid(cdiv(M, rb), cdiv(N, threads));
     DevBands bd = bands_of(c);
-    if (c.mask_option != 0 && c.f_finite) {
-      // R's row-occupancy masks; one warp per (row block, column group)
-      // visiting only the d where its columns of R are non-zero
-      const int ng = cdiv(N, 32), nseg = cdiv(D, 32);
-      k_row_masks<double><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), 1), 256, 0, c.st>>>(c.R.p, 0, D, N, c.rmask.p);
-      post_launch(c);
-      const dim3 grid(cdiv(M, rb * kTgRows), ng), blk(32, kTgRows);
-      if (rb == 8) k_trans_df_grp<8><<<grid, blk, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p, c.rmask.p);
-      else if (rb == 4) k_trans_df_grp<4><<<grid, blk, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p, c.rmask.p);
-      else k_trans_df_grp<2><<<grid, blk, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p, c.rmask.p);
-    } else {
-      const int threads = 32 * std::min(kDfColWarps, cdiv(N, 32));
-      const dim3 grid(cdiv(M, rb), cdiv(N, threads));
-      if (rb == 8) k_trans_df<8><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
-      else if (rb == 4) k_trans_df<4><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
-      else k_trans_df<2><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
-    }
+    if (rb == 8) k_trans_df<8><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
+    else if (rb == 4) k_trans_df<4><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
+    else k_trans_df<2><<<grid, threads, 0, c.st>>>(bd, c.tdf.p, c.rdf.p, c.X.p, c2g, g, c.Gf.p);
     post_launch(c);
     if (!c.fullspace) {
       k_reduced_from_full<<<M, std::min(256, std::max(32, cdiv(N, 32) * 32)), 0, c.st>>>(c.Gf.p, c.maxr.p, N, c.G.p);
