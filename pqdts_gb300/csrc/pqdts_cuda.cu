@@ -357,6 +357,13 @@ struct pqdts_ctx {
   // up to kBatchLS stacked inputs) and whether they are used: on unless the
   // option row_masks is 0 or F holds a value that is not finite
   pqdts::DBuf<uint32_t> xmask, rmask;
+  // the transposed FP64 products with masks: F^T in tiles of 32 rows
+  // (k_ftile_build; built when every column of F is contiguous in d and F is
+  // finite) and R's column masks and occupied-row lists (k_col_masks,
+  // k_col_lists)
+  pqdts::DBuf<double> ftile;
+  pqdts::DBuf<int32_t> ftile_lo, ftile_hi, ccnt, clist;
+  pqdts::DBuf<int64_t> ftile_off;
   int mask_option = 1;
   // option count_fmas: the masked FP64 products add the FMAs they execute
   // (per output lane) to fmacount[0] (forward) and [1] (transposed)
@@ -631,7 +638,43 @@ static void setup_device(Ctx& c) {
   c.sqd.alloc(M);
   c.f_finite = std::all_of(h.fval.begin(), h.fval.end(), [](double v) { return std::isfinite(v); });
   c.xmask.alloc((size_t)kBatchLS * cdiv(N, 32) * cdiv(M, 32));
-  c.rmask.alloc((size_t)cdiv(N, 32) * cdiv(D, 32));
+  c.rmask.alloc((size_t)N * cdiv(D, 32));
+  if (c.t_contiguous && c.f_finite) {
+    // F^T's 32-row tiles: the union of the tile's column ranges of d each
+    const int64_t nb = cdiv(M, 32);
+    std::vector<int32_t> lo(nb), hi(nb);
+    std::vector<int64_t> off(nb + 1, 0);
+    for (int64_t b = 0; b < nb; ++b) {
+      int32_t l = INT32_MAX, u = 0;
+      for (int64_t i = b * 32; i < std::min(M, b * 32 + 32); ++i) {
+        const int64_t e0 = h.tptr[i], e1 = h.tptr[i + 1];
+        if (e1 > e0) {
+          l = std::min(l, h.tidx[e0]);
+          u = std::max(u, h.tidx[e1 - 1] + 1);
+        }
+      }
+      if (l >= u) l = u = 0;
+      lo[b] = l;
+      hi[b] = u;
+      off[b + 1] = off[b] + (int64_t)(u - l) * 32;
+    }
+    c.ftile_lo.upload(lo.data(), nb, c.st, &c.h2d);
+    c.ftile_hi.upload(hi.data(), nb, c.st, &c.h2d);
+    c.ftile_off.upload(off.data(), nb + 1, c.st, &c.h2d);
+    c.ftile.alloc(std::max<int64_t>(off[nb], 1));
+    k_ftile_build<<<(unsigned)nb, 256, 0, c.st>>>(bands_of(c), c.tval.p, c.ftile_lo.p, c.ftile_hi.p, c.ftile_off.p,
+                                                   c.ftile.p);
+    post_launch(c);
+    c.ccnt.alloc((size_t)N * (cdiv(D, 32) + 1));
+    c.clist.alloc((size_t)N * D);
+  } else {
+    c.ftile.release();
+    c.ftile_lo.release();
+    c.ftile_hi.release();
+    c.ftile_off.release();
+    c.ccnt.release();
+    c.clist.release();
+  }
   c.fmacount.alloc(2);
   CK(cudaMemsetAsync(c.fmacount.p, 0, 2 * sizeof(unsigned long long), c.st));
   CK(cudaFuncSetAttribute(k_condat_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCondatSmemMax));
@@ -890,17 +933,24 @@ static void launch_trans_shape(Ctx& c, TransShape sh, const T* tv, const T* R, c
   DevBands bd = bands_of(c);
   const int RB = rows_per_block((int)c.h.N);
   int raw = 0;
-  if (std::is_same<T, double>::value && c.mask_option != 0 && c.f_finite && c.t_contiguous && c.rmask.p != nullptr) {
-    // FP64: the sums by (row, column group) warps visiting only the d where
-    // the group's columns of R are non-zero (R's row-occupancy masks; the
-    // same bits), then k_trans's epilogue on them
-    const int N = (int)c.h.N, D = (int)c.h.D, ng = cdiv(N, 32), nseg = cdiv(D, 32);
-    k_row_masks<T><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), 1), 256, 0, c.st>>>(R, 0, D, N, c.rmask.p);
-    post_launch(c);
-    k_trans_grp<T><<<dim3(cdiv(M, kTgRows), ng), dim3(32, kTgRows), 0, c.st>>>(bd, tv, R, c.rmask.p, G, pred,
-                                                c.count_fmas ? c.fmacount.p + 1 : nullptr);
-    post_launch(c);
-    raw = 1;
+  if constexpr (std::is_same<T, double>::value) {
+    if (c.mask_option != 0 && c.ftile.p != nullptr && tv == c.tval.p) {
+      // FP64: the sums by (column n, 32-row tile of F^T) warps visiting only
+      // the d where R[d, n] != 0 (R's column lists; the same bits), then
+      // k_trans's epilogue on them
+      const int N = (int)c.h.N, D = (int)c.h.D, nseg = cdiv(D, 32);
+      k_col_masks<T><<<cdiv((int64_t)nseg * N, 256), 256, 0, c.st>>>(R, D, N, c.rmask.p);
+      post_launch(c);
+      k_col_lists<<<cdiv((int64_t)N * 32, 256), 256, 0, c.st>>>(c.rmask.p, D, N, c.ccnt.p, c.clist.p);
+      post_launch(c);
+      k_trans_col<T><<<dim3(cdiv(N, kTcWarps), cdiv(M, 32)), dim3(32, kTcWarps), 0, c.st>>>(
+          M, N, D, c.ftile.p, c.ftile_lo.p, c.ftile_hi.p, c.ftile_off.p, R, c.rmask.p, c.ccnt.p, c.clist.p, G, pred,
+          c.count_fmas ? c.fmacount.p + 1 : nullptr);
+      post_launch(c);
+      raw = 1;
+    }
+  }
+  if (raw) {
   } else if (sh.rows && W == nullptr && c.t_contiguous && RB > 0) {
     const int threads = cdiv((int64_t)RB * c.h.N, 32) * 32;
     k_trans_rows<T, HVP><<<cdiv(M, RB), threads, 0, c.st>>>(bd, tv, RB, R, V, rs, c.maxr.p, reduced, c2gam, ik, G,

@@ -331,15 +331,32 @@ def test_row_masks_forward_product(built, request, which, precision):
 
 def test_row_masks_fma_counts(built):
     """The masked FP64 products count the FMAs they execute (option
-    count_fmas): with a direction of no zeros every band term runs (nnz * N
-    in each product, as the full chains); with Pi-like zeros (7 groups of 32
-    columns, two of them empty) fewer, and the Hessian product is the same
-    bits."""
+    count_fmas): with a direction of no zeros the forward product runs every
+    band term (nnz * N, as the full chains) and the transposed one every term
+    of F^T's 32-row tiles (each tile spans the union of its 32 columns'
+    ranges of d, zero-filled: a little over nnz * N); with Pi-like zeros (7
+    groups of 32 columns, two of them empty) fewer, and the Hessian product
+    is the same bits."""
     import pqdts_gb300 as pq
     from pqdts_gb300 import synth
 
     inst = synth.make_instance(M=300, N=200, D=600, xmax=250.0, eta=0.8, shots=10**6, gamma=1e-4, eps=1e-6, seed=8)
     nnz_n = int(inst.nnz) * inst.N
+    # F^T's tiles: rows i of 32 b .. 32 b + 31, d over the union of their columns' ranges
+    rows = np.flatnonzero(inst.band_lo >= 0)
+    clo = np.full(inst.M, inst.D)
+    chi = np.zeros(inst.M, dtype=np.int64)
+    for d in rows:
+        a, b = inst.band_lo[d], inst.band_hi[d] + 1
+        clo[a:b] = np.minimum(clo[a:b], d)
+        chi[a:b] = np.maximum(chi[a:b], d + 1)
+    tile_terms = 0
+    for b0 in range(0, inst.M, 32):
+        lo, hi = clo[b0 : b0 + 32], chi[b0 : b0 + 32]
+        if (hi > lo).any():
+            tile_terms += (hi[hi > lo].max() - lo[hi > lo].min()) * min(32, inst.M - b0)
+    tile_n = int(tile_terms) * inst.N
+    assert tile_n >= nnz_n
     rng = np.random.default_rng(4)
     dense = np.asfortranarray(rng.standard_normal((inst.M, inst.N)) + 3.0)  # no zeros
     sparse = _sparse_x(inst, 6)
@@ -353,6 +370,6 @@ def test_row_masks_fma_counts(built):
             counts.append((s.get_option("fmas.forward") - f0, s.get_option("fmas.transposed") - t0))
         s.set_option("row_masks", 0)
         H0 = s.BF(sparse)
-    assert counts[0] == (nnz_n, nnz_n), (counts, nnz_n)
-    assert 0 < counts[1][0] < nnz_n and 0 < counts[1][1] <= nnz_n, counts
+    assert counts[0] == (nnz_n, tile_n), (counts, nnz_n, tile_n)
+    assert 0 < counts[1][0] < nnz_n and 0 < counts[1][1] < tile_n, counts
     assert np.array_equal(H, H0)
