@@ -353,17 +353,24 @@ struct pqdts_ctx {
   // objective checks (option -1 auto = on, 0 native FP64, 1 on): F and F^T
   // values, and the split X and R operands, as (hi, lo) pairs
   pqdts::DBuf<float2> fdf, tdf, xdf, rdf;
-  // row-occupancy masks of the FP64 forward products' operand (k_row_masks,
-  // up to kBatchLS stacked inputs) and whether they are used: on unless the
-  // option row_masks is 0 or F holds a value that is not finite
-  pqdts::DBuf<uint32_t> xmask, rmask;
-  // the transposed FP64 products with masks: F^T in tiles of 32 rows
-  // (k_ftile_build; built when every column of F is contiguous in d and F is
-  // finite) and R's column masks and occupied-row lists (k_col_masks,
-  // k_col_lists)
+  // row-occupancy masks of the double-FP32 forward products' operand
+  // (k_row_masks, up to kBatchLS stacked inputs)
+  pqdts::DBuf<uint32_t> xmask;
+  // Zero-skipping products (option row_masks, on unless 0; only where F is
+  // finite).  The transposed FP64 products: F^T in tiles of 32 rows
+  // (k_ftile_build; built when every column of F is contiguous in d) and R's
+  // column masks and occupied-row lists (k_col_masks, k_col_lists)
+  pqdts::DBuf<uint32_t> rmask;
   pqdts::DBuf<double> ftile;
   pqdts::DBuf<int32_t> ftile_lo, ftile_hi, ccnt, clist;
   pqdts::DBuf<int64_t> ftile_off;
+  // the forward FP64 products with masks: F in tiles of 32 rows
+  // (k_fwtile_build; built when F is finite) and X's column masks and
+  // occupied-row lists for up to kBatchLS stacked inputs
+  pqdts::DBuf<double> fwtile;
+  pqdts::DBuf<int32_t> fwtile_lo, fwtile_hi, xccnt, xclist;
+  pqdts::DBuf<int64_t> fwtile_off;
+  pqdts::DBuf<uint32_t> xcmask;
   int mask_option = 1;
   // option count_fmas: the masked FP64 products add the FMAs they execute
   // (per output lane) to fmacount[0] (forward) and [1] (transposed)
@@ -675,6 +682,44 @@ static void setup_device(Ctx& c) {
     c.ccnt.release();
     c.clist.release();
   }
+  if (c.f_finite) {
+    // F's 32-row tiles: the union of the tile's row bands each
+    const int64_t nb = cdiv(D, 32);
+    std::vector<int32_t> lo(nb), hi(nb);
+    std::vector<int64_t> off(nb + 1, 0);
+    for (int64_t b = 0; b < nb; ++b) {
+      int32_t l = INT32_MAX, u = 0;
+      for (int64_t d = b * 32; d < std::min(D, b * 32 + 32); ++d) {
+        if (h.flo[d] >= 0 && h.fw[d] > 0) {
+          l = std::min(l, h.flo[d]);
+          u = std::max(u, h.flo[d] + h.fw[d]);
+        }
+      }
+      if (l >= u) l = u = 0;
+      lo[b] = l;
+      hi[b] = u;
+      off[b + 1] = off[b] + (int64_t)(u - l) * 32;
+    }
+    c.fwtile_lo.upload(lo.data(), nb, c.st, &c.h2d);
+    c.fwtile_hi.upload(hi.data(), nb, c.st, &c.h2d);
+    c.fwtile_off.upload(off.data(), nb + 1, c.st, &c.h2d);
+    c.fwtile.alloc(std::max<int64_t>(off[nb], 1));
+    k_fwtile_build<<<(unsigned)nb, 256, 0, c.st>>>(bands_of(c), c.fval.p, c.fwtile_lo.p, c.fwtile_hi.p,
+                                                    c.fwtile_off.p, c.fwtile.p);
+    post_launch(c);
+    c.xcmask.alloc((size_t)kBatchLS * N * cdiv(M, 32));
+    c.xccnt.alloc((size_t)kBatchLS * N * (cdiv(M, 32) + 1));
+    c.xclist.alloc((size_t)kBatchLS * N * M);
+    CK(cudaStreamSynchronize(c.st));  // host staging vectors go out of scope
+  } else {
+    c.fwtile.release();
+    c.fwtile_lo.release();
+    c.fwtile_hi.release();
+    c.fwtile_off.release();
+    c.xcmask.release();
+    c.xccnt.release();
+    c.xclist.release();
+  }
   c.fmacount.alloc(2);
   CK(cudaMemsetAsync(c.fmacount.p, 0, 2 * sizeof(unsigned long long), c.st));
   CK(cudaFuncSetAttribute(k_condat_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCondatSmemMax));
@@ -796,15 +841,23 @@ static void launch_fwd(Ctx& c, const T* fv, const T* X, int64_t xstride, const d
   const int N = (int)c.h.N, D = (int)c.h.D;
   DevBands bd = bands_of(c);
   const int RB = rows_per_block(N);
-  if (std::is_same<T, double>::value && c.mask_option != 0 && c.f_finite && c.xmask.p != nullptr) {
-    // FP64: the column-tiled form visiting only the rows of X where a
-    // warp's column group is non-zero (the same bits)
-    const int M = (int)c.h.M, ng = cdiv(N, 32), nseg = cdiv(M, 32);
-    k_row_masks<T><<<dim3(cdiv((int64_t)ng * nseg * 32, 256), B), 256, 0, c.st>>>(X, xstride, M, N, c.xmask.p);
-    post_launch(c);
-    k_fwd<T, MODE><<<dim3(cdiv(N, kBX), cdiv(D, kBY), B), dim3(kBX, kBY), 0, c.st>>>(bd, fv, X, xstride, P, R, nullptr,
-                                                                                    pred, c.xmask.p,
-                                                                                    c.count_fmas ? c.fmacount.p : nullptr);
+  bool masked = false;
+  if constexpr (std::is_same<T, double>::value) {
+    if (c.mask_option != 0 && c.fwtile.p != nullptr && fv == c.fval.p) {
+      // FP64: (column n, 32-row tile of F) warps visiting only the rows of
+      // X where X[i, n] != 0 (X's column lists; the same bits)
+      const int M = (int)c.h.M, nseg = cdiv(M, 32);
+      k_col_masks<T><<<dim3(cdiv((int64_t)nseg * N, 256), B), 256, 0, c.st>>>(X, xstride, M, N, c.xcmask.p);
+      post_launch(c);
+      k_col_lists<<<dim3(cdiv((int64_t)N * 32, 256), B), 256, 0, c.st>>>(c.xcmask.p, M, N, c.xccnt.p, c.xclist.p);
+      post_launch(c);
+      k_fwd_col<T, MODE><<<dim3(cdiv(N, kTcWarps), cdiv(D, 32), B), dim3(32, kTcWarps), 0, c.st>>>(
+          M, N, D, c.fwtile.p, c.fwtile_lo.p, c.fwtile_hi.p, c.fwtile_off.p, X, xstride, c.xcmask.p, c.xccnt.p,
+          c.xclist.p, P, R, pred, c.count_fmas ? c.fmacount.p : nullptr);
+      masked = true;
+    }
+  }
+  if (masked) {
   } else if ((rows < 0 ? c.sched.fwd_rows : rows) && RB > 0) {
     const int threads = cdiv((int64_t)RB * N, 32) * 32;
     k_fwd_rows<T, MODE><<<dim3(cdiv(D, RB), B), threads, 0, c.st>>>(bd, fv, X, xstride, P, R, RB, pred);
@@ -939,7 +992,7 @@ static void launch_trans_shape(Ctx& c, TransShape sh, const T* tv, const T* R, c
       // the d where R[d, n] != 0 (R's column lists; the same bits), then
       // k_trans's epilogue on them
       const int N = (int)c.h.N, D = (int)c.h.D, nseg = cdiv(D, 32);
-      k_col_masks<T><<<cdiv((int64_t)nseg * N, 256), 256, 0, c.st>>>(R, D, N, c.rmask.p);
+      k_col_masks<T><<<cdiv((int64_t)nseg * N, 256), 256, 0, c.st>>>(R, 0, D, N, c.rmask.p);
       post_launch(c);
       k_col_lists<<<cdiv((int64_t)N * 32, 256), 256, 0, c.st>>>(c.rmask.p, D, N, c.ccnt.p, c.clist.p);
       post_launch(c);

@@ -331,12 +331,11 @@ def test_row_masks_forward_product(built, request, which, precision):
 
 def test_row_masks_fma_counts(built):
     """The masked FP64 products count the FMAs they execute (option
-    count_fmas): with a direction of no zeros the forward product runs every
-    band term (nnz * N, as the full chains) and the transposed one every term
-    of F^T's 32-row tiles (each tile spans the union of its 32 columns'
-    ranges of d, zero-filled: a little over nnz * N); with Pi-like zeros (7
-    groups of 32 columns, two of them empty) fewer, and the Hessian product
-    is the same bits."""
+    count_fmas): with a direction of no zeros they run every term of F's
+    32-row tiles (forward; each tile spans the union of its 32 rows' bands,
+    zero-filled) and of F^T's (transposed): a little over nnz * N each; with
+    Pi-like zeros (7 groups of 32 columns, two of them empty) fewer, and the
+    Hessian product is the same bits."""
     import pqdts_gb300 as pq
     from pqdts_gb300 import synth
 
@@ -356,7 +355,15 @@ def test_row_masks_fma_counts(built):
         if (hi > lo).any():
             tile_terms += (hi[hi > lo].max() - lo[hi > lo].min()) * min(32, inst.M - b0)
     tile_n = int(tile_terms) * inst.N
-    assert tile_n >= nnz_n
+    # F's tiles: rows d of 32 b .. 32 b + 31 (every row a lane), i over the union of their bands
+    ftile_terms = 0
+    for b0 in range(0, inst.D, 32):
+        lo, hi = inst.band_lo[b0 : b0 + 32], inst.band_hi[b0 : b0 + 32] + 1
+        ok = lo >= 0
+        if ok.any():
+            ftile_terms += (hi[ok].max() - lo[ok].min()) * min(32, inst.D - b0)
+    ftile_n = int(ftile_terms) * inst.N
+    assert tile_n >= nnz_n and ftile_n >= nnz_n
     rng = np.random.default_rng(4)
     dense = np.asfortranarray(rng.standard_normal((inst.M, inst.N)) + 3.0)  # no zeros
     sparse = _sparse_x(inst, 6)
@@ -370,6 +377,6 @@ def test_row_masks_fma_counts(built):
             counts.append((s.get_option("fmas.forward") - f0, s.get_option("fmas.transposed") - t0))
         s.set_option("row_masks", 0)
         H0 = s.BF(sparse)
-    assert counts[0] == (nnz_n, tile_n), (counts, nnz_n, tile_n)
-    assert 0 < counts[1][0] < nnz_n and 0 < counts[1][1] < tile_n, counts
+    assert counts[0] == (ftile_n, tile_n), (counts, nnz_n, ftile_n, tile_n)
+    assert 0 < counts[1][0] < ftile_n and 0 < counts[1][1] < tile_n, counts
     assert np.array_equal(H, H0)
