@@ -178,6 +178,10 @@ int pqdts_cuda_dL(pqdts_ctx* ctx, double* G_colmajor);             /* dL, pqdts.
 int pqdts_cuda_redO(pqdts_ctx* ctx, double* O_ND);                 /* redO local part, 707-736 */
 int pqdts_cuda_BF(pqdts_ctx* ctx, const double* V_colmajor, double* HV_colmajor); /* BF, 246-342 (FP64) */
 int pqdts_cuda_Bdiag(pqdts_ctx* ctx, double* BD_colmajor);         /* Bdiag, 208-244 */
+/* pdot (589-614): sum(A*B) over the problem's M x N arrays.  FP64 problems
+ * add in the reference's order (one chain per column over the rows, the
+ * columns' results then added in ascending order), bit for bit. */
+int pqdts_cuda_pdot(pqdts_ctx* ctx, const double* A_colmajor, const double* B_colmajor, double* out);
 /* BF in the mixed-precision solver's arithmetic (FP32 values and
  * accumulation; PQDTS_MIXED problems only): the CG's Hessian product. */
 int pqdts_cuda_BF32(pqdts_ctx* ctx, const double* V_colmajor, double* HV_colmajor);

@@ -66,6 +66,7 @@ def lib():
         "pqdts_cuda_BF": [p, p, p],
         "pqdts_cuda_BF32": [p, p, p],
         "pqdts_cuda_Bdiag": [p, p],
+        "pqdts_cuda_pdot": [p, p, p, C.POINTER(d)],
         "pqdts_cuda_doproj": [p],
         "pqdts_cuda_doproj2": [p, C.POINTER(d)],
         "pqdts_cuda_conv_test": [p, C.POINTER(d)],
@@ -238,6 +239,14 @@ class Solver:
         B = np.empty((self.M, self.N), order="F")
         self._check(self._L.pqdts_cuda_Bdiag(self.h, _ptr(B)), "Bdiag")
         return B
+
+    def pdot(self, A, B):
+        """sum(A*B) over the problem's M x N arrays (pdot, pqdts.f90:589-614)."""
+        A = np.asfortranarray(A, np.float64)
+        B = np.asfortranarray(B, np.float64)
+        out = C.c_double()
+        self._check(self._L.pqdts_cuda_pdot(self.h, _ptr(A), _ptr(B), C.byref(out)), "pdot")
+        return out.value
 
     def doproj(self):
         self._check(self._L.pqdts_cuda_doproj(self.h), "doproj")

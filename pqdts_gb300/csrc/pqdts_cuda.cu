@@ -787,13 +787,13 @@ static void objective_combine(Ctx& c, const double* Xs, int B) {
   const int M = (int)c.h.M, N = (int)c.h.N, D = (int)c.h.D;
   if (c.exact) {
     double* out = c.h.gam != 0 ? c.lred.p : c.lsout.p;
-    k_seqsum<<<1, 32, 0, c.st>>>(c.srow.p, D, nullptr, out, B, nullptr);
+    k_seqsum<<<B, 32, 0, c.st>>>(c.srow.p, D, nullptr, out, B, nullptr);
     post_launch(c);
     if (c.h.gam != 0) {
-      k_colchain<1><<<dim3(cdiv(N, 32), B), 256, 0, c.st>>>(Xs, nullptr, (int64_t)M * N, M, N, c.h.gam, c.gcol.p,
-                                                           nullptr, nullptr);
+      k_colchain<1><<<dim3(cdiv(N, kChainWarps), B), 32 * kChainWarps, 0, c.st>>>(
+          Xs, nullptr, (int64_t)M * N, M, N, c.h.gam, c.gcol.p, nullptr, nullptr);
       post_launch(c);
-      k_seqsum<<<1, 32, 0, c.st>>>(c.gcol.p, N, c.lred.p, c.lsout.p, B, nullptr);
+      k_seqsum<<<B, 32, 0, c.st>>>(c.gcol.p, N, c.lred.p, c.lsout.p, B, nullptr);
       post_launch(c);
     }
     CK(cudaMemsetAsync(c.lsout.p + kBatchLS, 0, B * sizeof(double), c.st));
@@ -1099,8 +1099,8 @@ static void dot_dev(Ctx& c, const double* a, const double* b, double* out, const
   const int M = (int)c.h.M, N = (int)c.h.N;
   if (c.exact) {
     // column chains, then (last block) their ascending sum into out
-    k_colchain<0><<<dim3(cdiv(N, 32), 1), 256, 0, c.st>>>(a, b, 0, M, N, 0.0, c.colbuf.p, nullptr, pred, out, 1,
-                                                          c.counters.p + 2);
+    k_colchain<0><<<dim3(cdiv(N, kChainWarps), 1), 32 * kChainWarps, 0, c.st>>>(a, b, 0, M, N, 0.0, c.colbuf.p,
+                                                                                nullptr, pred, out, 1, c.counters.p + 2);
     post_launch(c);
     return;
   }
@@ -1112,12 +1112,12 @@ static void dot_dev(Ctx& c, const double* a, const double* b, double* out, const
 }
 
 // Two pdots of the FP64 CG at once: a.b -> out_ab, a.a -> out_aa, where
-// out_aa = out_ab + ostride (two chains over one staged tile, two warps).
+// out_aa = out_ab + ostride (two chains per column in one warp).
 static void dot2_exact(Ctx& c, const double* a, const double* b, double* out_ab, int ostride,
                        const double* pred) {
   const int M = (int)c.h.M, N = (int)c.h.N;
-  k_colchain<2><<<dim3(cdiv(N, 32), 1), 256, 0, c.st>>>(a, b, 0, M, N, 0.0, c.colbuf.p, c.colbuf.p + N, pred,
-                                                        out_ab, ostride, c.counters.p + 3);
+  k_colchain<2><<<dim3(cdiv(N, kChainWarps), 1), 32 * kChainWarps, 0, c.st>>>(
+      a, b, 0, M, N, 0.0, c.colbuf.p, c.colbuf.p + N, pred, out_ab, ostride, c.counters.p + 3);
   post_launch(c);
 }
 
@@ -3181,6 +3181,25 @@ int pqdts_cuda_BF32(pqdts_ctx* c, const double* V, double* HV) {
     c->d2h += (int64_t)rm.size() * 4;
     for (int64_t i = 0; i < M; ++i)
       for (int64_t n = 0; n < N; ++n) HV[i + n * M] = rm[(size_t)i * N + n];
+  });
+}
+
+int pqdts_cuda_pdot(pqdts_ctx* c, const double* A, const double* B, double* out) {
+  return guarded(c, [&] {
+    pqdts::need_problem(*c);
+    const int64_t M = c->h.M, N = c->h.N;
+    std::vector<double> ra((size_t)M * N), rb((size_t)M * N);
+    for (int64_t i = 0; i < M; ++i)
+      for (int64_t n = 0; n < N; ++n) {
+        ra[(size_t)i * N + n] = A[i + n * M];
+        rb[(size_t)i * N + n] = B[i + n * M];
+      }
+    auto& b = c->cg64;
+    CK(cudaMemcpyAsync(b.p.p, ra.data(), ra.size() * 8, cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(b.z.p, rb.data(), rb.size() * 8, cudaMemcpyHostToDevice, c->st));
+    pqdts::dot_dev(*c, b.p.p, b.z.p, c->sc.p + pqdts::SC_TMP);
+    CK(cudaMemcpyAsync(out, c->sc.p + pqdts::SC_TMP, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
   });
 }
 

@@ -132,6 +132,14 @@ module pqdts_cuda_mod
       real(c_double) :: BD(*)
     end function
 
+    ! function pdot(a, b), pqdts.f90:589: sum(a*b) in the reference's order
+    integer(c_int32_t) function pqdts_cuda_pdot(ctx, A, B, res) bind(C, name="pqdts_cuda_pdot")
+      import :: c_int32_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: A(*), B(*)
+      real(c_double) :: res
+    end function
+
     ! subroutine doproj(X), pqdts.f90:1120
     integer(c_int32_t) function pqdts_cuda_doproj(ctx) bind(C, name="pqdts_cuda_doproj")
       import :: c_int32_t, c_ptr

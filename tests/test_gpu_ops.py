@@ -380,3 +380,49 @@ def test_row_masks_fma_counts(built):
     assert counts[0] == (ftile_n, tile_n), (counts, nnz_n, ftile_n, tile_n)
     assert 0 < counts[1][0] < ftile_n and 0 < counts[1][1] < tile_n, counts
     assert np.array_equal(H, H0)
+
+
+def _chain_cases(M, N, seed):
+    """Arrays whose pdot chains meet every branch of the warp-parallel exact
+    chain: products that tie at the accumulator's grid (3 * (2^52 + 1)
+    scaled), partial sums crossing binades up and down and cancelling to
+    exactly zero, signed zeros, underflowing products and huge terms."""
+    rng = np.random.default_rng(seed)
+    A = rng.standard_normal((M, N)) * 2.0 ** rng.integers(-40, 40, (M, N))
+    B = rng.standard_normal((M, N))
+    k = rng.random((M, N))
+    t = k < 0.08  # ties
+    A[t] = 3.0 * 2.0 ** rng.integers(-20, 20, t.sum())
+    B[t] = float((1 << 52) + 1)
+    z = (k >= 0.08) & (k < 0.16)  # signed zeros
+    A[z] = rng.choice([0.0, -0.0], z.sum())
+    u = (k >= 0.16) & (k < 0.2)  # products that underflow
+    A[u] = 1e-200
+    B[u] = -1e-200
+    c = (k >= 0.2) & (k < 0.26)  # cancel the column so far
+    A[c] = 1.0
+    B[c] = 0.0
+    h = (k >= 0.26) & (k < 0.27)  # huge terms (no overflow: a few per column)
+    A[h] = 1e300
+    B[h] = rng.choice([1.0, -1.0], h.sum())
+    for n in range(N):
+        for i in np.flatnonzero(c[:, n]):
+            B[i, n] = -float(np.sum(A[:i, n] * B[:i, n]))  # roughly cancels: the chain passes near 0
+    return np.asfortranarray(A), np.asfortranarray(B)
+
+
+@pytest.mark.parametrize("which", ["cfg1", "small"])
+def test_pdot_exact_chains(built, request, which):
+    """pdot through the warp-parallel exact chains (k_colchain) equals the
+    oracle's sequential pdot bit for bit, on ordinary arrays, on arrays made
+    to hit every fallback branch, and on a = b."""
+    inst = request.getfixturevalue(which)
+    s, o = _pair(inst)
+    rng = np.random.default_rng(21)
+    cases = [(_random_x(inst, 22), _random_x(inst, 23)),
+             (np.asfortranarray(rng.standard_normal((inst.M, inst.N))),) * 2]
+    for seed in range(4):
+        cases.append(_chain_cases(inst.M, inst.N, 30 + seed))
+    for A, B in cases:
+        g, r = s.pdot(A, B), o.pdot(A, B)
+        assert np.float64(g).tobytes() == np.float64(r).tobytes(), (g, r)
