@@ -359,7 +359,7 @@ struct pqdts_ctx {
   // Zero-skipping products (option row_masks, on unless 0; only where F is
   // finite).  The transposed FP64 products: F^T in tiles of 32 rows
   // (k_ftile_build; built when every column of F is contiguous in d) and R's
-  // column masks and occupied-row lists (k_col_masks, k_col_lists)
+  // column masks and occupied-row lists (k_col_index)
   pqdts::DBuf<uint32_t> rmask;
   pqdts::DBuf<double> ftile;
   pqdts::DBuf<int32_t> ftile_lo, ftile_hi, ccnt, clist;
@@ -841,24 +841,22 @@ static void launch_fwd(Ctx& c, const T* fv, const T* X, int64_t xstride, const d
   const int N = (int)c.h.N, D = (int)c.h.D;
   DevBands bd = bands_of(c);
   const int RB = rows_per_block(N);
-  bool masked = false;
   if constexpr (std::is_same<T, double>::value) {
     if (c.mask_option != 0 && c.fwtile.p != nullptr && fv == c.fval.p) {
       // FP64: (column n, 32-row tile of F) warps visiting only the rows of
       // X where X[i, n] != 0 (X's column lists; the same bits)
-      const int M = (int)c.h.M, nseg = cdiv(M, 32);
-      k_col_masks<T><<<dim3(cdiv((int64_t)nseg * N, 256), B), 256, 0, c.st>>>(X, xstride, M, N, c.xcmask.p);
-      post_launch(c);
-      k_col_lists<<<dim3(cdiv((int64_t)N * 32, 256), B), 256, 0, c.st>>>(c.xcmask.p, M, N, c.xccnt.p, c.xclist.p);
+      const int M = (int)c.h.M;
+      k_col_index<T><<<dim3(cdiv(N, kIndexWarps), B), 32 * kIndexWarps, 0, c.st>>>(X, xstride, M, N, c.xcmask.p,
+                                                                                  c.xccnt.p, c.xclist.p);
       post_launch(c);
       k_fwd_col<T, MODE><<<dim3(cdiv(N, kTcWarps), cdiv(D, 32), B), dim3(32, kTcWarps), 0, c.st>>>(
           M, N, D, c.fwtile.p, c.fwtile_lo.p, c.fwtile_hi.p, c.fwtile_off.p, X, xstride, c.xcmask.p, c.xccnt.p,
           c.xclist.p, P, R, pred, c.count_fmas ? c.fmacount.p : nullptr);
-      masked = true;
+      post_launch(c);
+      return;
     }
   }
-  if (masked) {
-  } else if ((rows < 0 ? c.sched.fwd_rows : rows) && RB > 0) {
+  if ((rows < 0 ? c.sched.fwd_rows : rows) && RB > 0) {
     const int threads = cdiv((int64_t)RB * N, 32) * 32;
     k_fwd_rows<T, MODE><<<dim3(cdiv(D, RB), B), threads, 0, c.st>>>(bd, fv, X, xstride, P, R, RB, pred);
   } else {
@@ -991,10 +989,9 @@ static void launch_trans_shape(Ctx& c, TransShape sh, const T* tv, const T* R, c
       // FP64: the sums by (column n, 32-row tile of F^T) warps visiting only
       // the d where R[d, n] != 0 (R's column lists; the same bits), then
       // k_trans's epilogue on them
-      const int N = (int)c.h.N, D = (int)c.h.D, nseg = cdiv(D, 32);
-      k_col_masks<T><<<cdiv((int64_t)nseg * N, 256), 256, 0, c.st>>>(R, 0, D, N, c.rmask.p);
-      post_launch(c);
-      k_col_lists<<<cdiv((int64_t)N * 32, 256), 256, 0, c.st>>>(c.rmask.p, D, N, c.ccnt.p, c.clist.p);
+      const int N = (int)c.h.N, D = (int)c.h.D;
+      k_col_index<T><<<cdiv(N, kIndexWarps), 32 * kIndexWarps, 0, c.st>>>(R, 0, D, N, c.rmask.p, c.ccnt.p,
+                                                                          c.clist.p);
       post_launch(c);
       k_trans_col<T><<<dim3(cdiv(N, kTcWarps), cdiv(M, 32)), dim3(32, kTcWarps), 0, c.st>>>(
           M, N, D, c.ftile.p, c.ftile_lo.p, c.ftile_hi.p, c.ftile_off.p, R, c.rmask.p, c.ccnt.p, c.clist.p, G, pred,
@@ -1112,11 +1109,11 @@ static void dot_dev(Ctx& c, const double* a, const double* b, double* out, const
 }
 
 // Two pdots of the FP64 CG at once: a.b -> out_ab, a.a -> out_aa, where
-// out_aa = out_ab + ostride (two chains per column in one warp).
+// out_aa = out_ab + ostride (a warp per chain, two per column).
 static void dot2_exact(Ctx& c, const double* a, const double* b, double* out_ab, int ostride,
                        const double* pred) {
   const int M = (int)c.h.M, N = (int)c.h.N;
-  k_colchain<2><<<dim3(cdiv(N, kChainWarps), 1), 32 * kChainWarps, 0, c.st>>>(
+  k_colchain<2><<<dim3(cdiv(N, kChainWarps / 2), 1), 32 * kChainWarps, 0, c.st>>>(
       a, b, 0, M, N, 0.0, c.colbuf.p, c.colbuf.p + N, pred, out_ab, ostride, c.counters.p + 3);
   post_launch(c);
 }
