@@ -505,9 +505,10 @@ def run_ours(args):
     assert replicas["identical"], f"ranks did different work on the same instance: {replicas}"
 
     # roofline of the dominant kernel: the transposed product of the CG's
-    # Hessian product (k_trans: F^T.(2 F.V) with the stencil, projection,
-    # mask and p.Hp epilogue), FP64-ALU bound; its forward product (k_fwd
-    # with row-occupancy masks) is reported beside it
+    # Hessian product (k_trans_col's sums of F^T.(2 F.V) over each column's
+    # non-zero rows, then k_trans's stencil, projection, mask and p.Hp
+    # epilogue), FP64-ALU bound; its forward product (k_fwd_col) is reported
+    # beside it
     nnz, N, M, D = inst.nnz, inst.N, inst.M, inst.D
     cg = st_t[0]["cg"]  # the CG iterations of the solve whose regions were timed
     bf_time = bf1[0] - bf0[0]
@@ -556,8 +557,9 @@ def run_ours(args):
                         "us_per_product": tfw / 5 * 1e6,
                         "executed_tflops": 2 * (d1 - d0) / tfw / 1e12 if tfw > 0 else None}}
     roofline = {
-        "kernel": "k_trans_grp + k_trans (the Hessian product's F^T.(2 F.V): sums over the non-zero rows of each "
-                  "32-column group of 2 F.V, then the stencil, projection, active-set mask epilogue)",
+        "kernel": "k_col_index + k_trans_col + k_trans (the Hessian product's F^T.(2 F.V): the occupied-row lists "
+                  "of each column of 2 F.V, sums over them by (column, 32-row tile of F^T) warps, then the stencil, "
+                  "projection, active-set mask epilogue)",
         "timed": "GPU events around each of the CG's transposed products in one solve of the workload "
                  "(region timers on)",
         "bound": "fp64" if prec == pq.FP64 else "fp32",
@@ -576,8 +578,8 @@ def run_ours(args):
                 "exact-zero terms, so this dense-equivalent rate exceeds the FP64 peak -- `executed` gives the rate "
                 "of the FMAs the kernels do execute",
         "forward_product": {
-            "kernel": "k_fwd with row-occupancy masks (F.V visiting only the rows where a warp's 32 columns of V "
-                      "are non-zero; the same bits as the full chain)",
+            "kernel": "k_col_index + k_fwd_col (F.V by (column of V, 32-row tile of F) warps visiting only the rows "
+                      "where that column of V is non-zero; the same bits as the full chain)",
             "us_per_launch": fw_time / fw_n * 1e6 if fw_n else None,
             "dense_equivalent_tflops": flops_one * fw_n / fw_time / 1e12 if fw_time > 0 else None,
             "note": "dense-equivalent flops over the time: above the FP64 peak because the skipped terms are exact "
@@ -713,9 +715,9 @@ def run_profile_case(case):
       solve64 / solvemix: one full benchmark solve (the launch list);
       fp64sp: the FP64 Hessian product (3x BF), 3x dL and 3x L at the
         FP64 solution of the workload (a sparse Pi, as the solve's iterates
-        are once in stage 2: the row-occupancy masks of the products see
-        the zeros they skip in the solve; the solve itself runs without
-        the masks, so the masked kernels' first launches are these); V =
+        are once in stage 2: the column lists of the products see the
+        zeros they skip in the solve; the solve itself runs without the
+        zero skipping, so the masked kernels' first launches are these); V =
         that Pi minus 1/N on its non-zeros, so it has the same zeros;
       solvemix3: the mixed solve of M=10000 N=1000 D=20000 to its own
         stopping rule conv < 1e-6 (no FP64 solve first: the launch list of

@@ -68,15 +68,17 @@ int pqdts_cuda_kernel_launches(pqdts_ctx* ctx, int64_t* count);
  *              form (one CTA per output tile, or persistent with
  *              double-buffered accumulators); "tc_splits1" -1 (autotuned) or
  *              1..8: K segments of the tensor-core F.V product.
- *   "row_masks" 1 (default) / 0: the FP64 banded products (and the mixed
- *              path's double-FP32 step check) visit only the rows of their
- *              operand where a warp's 32 columns hold a non-zero (the
+ *   "row_masks" 1 (default) / 0: the FP64 banded products visit, for
+ *              each column of their operand, only its non-zero rows (the
  *              iterate, the CG direction and the residual are mostly exact
- *              zeros); the FP64 results are the same bits either way (a
- *              skipped term adds +-0 to a sum that is never -0); off when F
- *              holds a value that is not finite.
- *   "count_fmas" 0 (default) / 1: the masked FP64 products count the
- *              FMAs they execute, read back as "fmas.forward" and
+ *              zeros), and the mixed path's double-FP32 step check only the
+ *              rows where a warp's 32 columns hold a non-zero; the FP64
+ *              results are the same bits either way (a skipped term adds
+ *              +-0 to a sum that is never -0); off when F holds a value
+ *              that is not finite.
+ *   "count_fmas" 0 (default) / 1: the zero-skipping FP64 products count
+ *              the FMAs they execute (per output lane, including the zero
+ *              fill of F's 32-row tiles), read back as "fmas.forward" and
  *              "fmas.transposed" (cumulative).
  *   "tc_screen" -1 (default) / 0: the mixed line search's probe products
  *              F.dX (its screen of step lengths, before the chosen step's
