@@ -993,9 +993,11 @@ static void launch_trans_shape(Ctx& c, TransShape sh, const T* tv, const T* R, c
       k_col_index<T><<<cdiv(N, kIndexWarps), 32 * kIndexWarps, 0, c.st>>>(R, 0, D, N, c.rmask.p, c.ccnt.p,
                                                                           c.clist.p);
       post_launch(c);
+      // with the active set (the CG's product), warps whose outputs are all
+      // masked by the epilogue skip their sums
       k_trans_col<T><<<dim3(cdiv(N, kTcWarps), cdiv(M, 32)), dim3(32, kTcWarps), 0, c.st>>>(
           M, N, D, c.ftile.p, c.ftile_lo.p, c.ftile_hi.p, c.ftile_off.p, R, c.rmask.p, c.ccnt.p, c.clist.p, G, pred,
-          c.count_fmas ? c.fmacount.p + 1 : nullptr);
+          c.count_fmas ? c.fmacount.p + 1 : nullptr, ik, reduced ? c.maxr.p : nullptr);
       post_launch(c);
       raw = 1;
     }
@@ -1754,8 +1756,8 @@ static void cg_solve(Ctx& c, CGBufs<T>& b, const T* fv, const T* tv, double bdfa
     }
     if constexpr (kF64)
       if (exact) dot_dev(c, b.p.p, b.Hp.p, c.sc.p + SC_V2, c.sc.p);
-    k_cg_step<T><<<g, 256, 0, c.st>>>(c.sc.p, c.sqd.p, M, N, b.p.p, b.Hp.p, b.sn.p, b.r.p, b.z.p, c.part.p,
-                                      c.part2.p);
+    k_cg_step<T><<<g, 256, 0, c.st>>>(c.sc.p, c.sqd.p, M, N, b.p.p, b.Hp.p, b.sn.p, b.r.p, b.z.p,
+                                      exact ? nullptr : c.part.p, exact ? nullptr : c.part2.p);
     post_launch(c);
     if (exact) {
       if constexpr (kF64) {
