@@ -575,8 +575,9 @@ def run_ours(args):
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
         "executed": executed,
         "note": "achieved = algorithmic (dense) flops 2 nnz N per launch over the time; the masked products skip "
-                "exact-zero terms, so this dense-equivalent rate exceeds the FP64 peak -- `executed` gives the rate "
-                "of the FMAs the kernels do execute",
+                "exact-zero terms and, in the CG, the outputs its active set masks, so this dense-equivalent rate "
+                "exceeds the FP64 peak -- `executed` gives the rate of the FMAs the kernels do execute (through "
+                "the BF entry point: no active set, no output skipped)",
         "forward_product": {
             "kernel": "k_col_index + k_fwd_col (F.V by (column of V, 32-row tile of F) warps visiting only the rows "
                       "where that column of V is non-zero; the same bits as the full chain)",
