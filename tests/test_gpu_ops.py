@@ -423,6 +423,16 @@ def test_pdot_exact_chains(built, request, which):
              (np.asfortranarray(rng.standard_normal((inst.M, inst.N))),) * 2]
     for seed in range(4):
         cases.append(_chain_cases(inst.M, inst.N, 30 + seed))
+    # steps whose exact sum falls just below a power of two (the correctly
+    # rounded sum is on the finer grid below it), one column each
+    ulp = 2.0 ** -52
+    A = np.zeros((inst.M, inst.N))
+    for n in range(inst.N):
+        k = 1 + n % 4
+        A[0, n] = (1.0 + k * ulp) * 2.0 ** (n % 7 - 3)
+        A[1, n] = -(k + 0.2 + 0.1 * (n % 3)) * ulp * 2.0 ** (n % 7 - 3)
+        A[2:, n] = np.random.default_rng(n).uniform(0, 1e-30, inst.M - 2)
+    cases.append((np.asfortranarray(A), np.asfortranarray(np.ones((inst.M, inst.N)))))
     for A, B in cases:
         g, r = s.pdot(A, B), o.pdot(A, B)
         assert np.float64(g).tobytes() == np.float64(r).tobytes(), (g, r)
